@@ -1,0 +1,1020 @@
+/*
+ * opx_oracle.c -- CPU FP64 oracle (test infrastructure only; see opx_oracle.h).
+ *
+ * Every function names the reference file:line it restates.  Reference paths
+ * are relative to pixi/src/main/java/org/openpixi/pixi/.
+ */
+#include "opx_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NG_MAX 18
+#define NA_MAX 9
+
+int orc_ng(int nc) { return nc == 3 ? 18 : 4; }
+int orc_na(int nc) { return nc == 3 ? 9 : 3; }
+
+/* ------------------------------------------------------------------------- */
+/* SU(2): quaternion e0 + i e_a sigma_a (math/SU2GroupElement.java:3-14)      */
+/* ------------------------------------------------------------------------- */
+
+/* SU2GroupElement.mult, math/SU2GroupElement.java:206-217 */
+static void su2_mult(const double *x, const double *a, double *b)
+{
+    double b0 = x[0] * a[0] - x[1] * a[1] - x[2] * a[2] - x[3] * a[3];
+    double b1 = x[0] * a[1] + x[1] * a[0] - x[2] * a[3] + x[3] * a[2];
+    double b2 = x[0] * a[2] + x[2] * a[0] - x[3] * a[1] + x[1] * a[3];
+    double b3 = x[0] * a[3] + x[3] * a[0] - x[1] * a[2] + x[2] * a[1];
+    b[0] = b0; b[1] = b1; b[2] = b2; b[3] = b3;
+}
+
+/* SU2AlgebraElement.getLink, math/SU2AlgebraElement.java:140-152 */
+static void su2_getlink(const double *v, double *u)
+{
+    double sum = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double mod = sqrt(sum) / 2;
+    double sinfakt;
+    if (mod < 1.E-20)
+        sinfakt = 0.0;
+    else
+        sinfakt = 0.5 / mod * sin(mod);
+    u[0] = cos(mod);
+    u[1] = v[0] * sinfakt;
+    u[2] = v[1] * sinfakt;
+    u[3] = v[2] * sinfakt;
+}
+
+/* SU2AlgebraElement.act, math/SU2AlgebraElement.java:159-172: proj(u X u^dagger) */
+static void su2_act(const double *v, const double *u, double *out)
+{
+    double xm[4] = {0.0, v[0] / 2, v[1] / 2, v[2] / 2};
+    double ua[4] = {u[0], -u[1], -u[2], -u[3]};
+    double t[4], r[4];
+    su2_mult(xm, ua, t);
+    su2_mult(u, t, r);
+    out[0] = 2 * r[1];
+    out[1] = 2 * r[2];
+    out[2] = 2 * r[3];
+}
+
+/* ------------------------------------------------------------------------- */
+/* SU(3): 3x3 complex, e[0..8] real parts, e[9..17] imaginary parts, row-major */
+/* (math/SU3GroupElement.java:3-11)                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Term order of SU3GroupElement.mult (math/SU3GroupElement.java:183-208).
+ * Entry k of l*r is the left-to-right sum of sign * r[ai] * l[ei] over the six
+ * (sign, ai, ei) triplets below.  The order is kept because the CPIC colour
+ * charge transport must be bit-identical to the reference. */
+static const signed char SU3_TERMS[18][6][3] = {
+    {{1, 0, 0}, {1, 3, 1}, {-1, 12, 10}, {-1, 15, 11}, {1, 6, 2}, {-1, 9, 9}},
+    {{1, 1, 0}, {1, 4, 1}, {-1, 13, 10}, {-1, 16, 11}, {1, 7, 2}, {-1, 10, 9}},
+    {{1, 2, 0}, {1, 5, 1}, {-1, 14, 10}, {-1, 17, 11}, {1, 8, 2}, {-1, 11, 9}},
+    {{-1, 9, 12}, {-1, 12, 13}, {-1, 15, 14}, {1, 0, 3}, {1, 3, 4}, {1, 6, 5}},
+    {{-1, 10, 12}, {-1, 13, 13}, {-1, 16, 14}, {1, 1, 3}, {1, 4, 4}, {1, 7, 5}},
+    {{-1, 11, 12}, {-1, 14, 13}, {-1, 17, 14}, {1, 2, 3}, {1, 5, 4}, {1, 8, 5}},
+    {{-1, 9, 15}, {-1, 12, 16}, {-1, 15, 17}, {1, 0, 6}, {1, 3, 7}, {1, 6, 8}},
+    {{-1, 10, 15}, {-1, 13, 16}, {-1, 16, 17}, {1, 1, 6}, {1, 4, 7}, {1, 7, 8}},
+    {{-1, 11, 15}, {-1, 14, 16}, {-1, 17, 17}, {1, 2, 6}, {1, 5, 7}, {1, 8, 8}},
+    {{1, 9, 0}, {1, 12, 1}, {1, 3, 10}, {1, 6, 11}, {1, 15, 2}, {1, 0, 9}},
+    {{1, 10, 0}, {1, 13, 1}, {1, 4, 10}, {1, 7, 11}, {1, 16, 2}, {1, 1, 9}},
+    {{1, 11, 0}, {1, 14, 1}, {1, 5, 10}, {1, 8, 11}, {1, 17, 2}, {1, 2, 9}},
+    {{1, 0, 12}, {1, 3, 13}, {1, 6, 14}, {1, 9, 3}, {1, 12, 4}, {1, 15, 5}},
+    {{1, 1, 12}, {1, 4, 13}, {1, 7, 14}, {1, 10, 3}, {1, 13, 4}, {1, 16, 5}},
+    {{1, 2, 12}, {1, 5, 13}, {1, 8, 14}, {1, 11, 3}, {1, 14, 4}, {1, 17, 5}},
+    {{1, 0, 15}, {1, 3, 16}, {1, 6, 17}, {1, 9, 6}, {1, 12, 7}, {1, 15, 8}},
+    {{1, 1, 15}, {1, 4, 16}, {1, 7, 17}, {1, 10, 6}, {1, 13, 7}, {1, 16, 8}},
+    {{1, 2, 15}, {1, 5, 16}, {1, 8, 17}, {1, 11, 6}, {1, 14, 7}, {1, 17, 8}},
+};
+
+static void su3_mult(const double *l, const double *r, double *out)
+{
+    double b[18];
+    for (int k = 0; k < 18; k++) {
+        const signed char(*t)[3] = SU3_TERMS[k];
+        double acc = (t[0][0] < 0 ? -r[t[0][1]] : r[t[0][1]]) * l[t[0][2]];
+        for (int m = 1; m < 6; m++) {
+            double prod = r[t[m][1]] * l[t[m][2]];
+            acc = t[m][0] < 0 ? acc - prod : acc + prod;
+        }
+        b[k] = acc;
+    }
+    memcpy(out, b, sizeof(b));
+}
+
+/* SU3GroupElement.adj, math/SU3GroupElement.java:101-131 */
+static void su3_adj(const double *e, double *b)
+{
+    double t[18];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            t[3 * i + j] = e[3 * j + i];
+            t[9 + 3 * i + j] = -e[9 + 3 * j + i];
+        }
+    memcpy(b, t, sizeof(t));
+}
+
+/* SU3GroupElement.proj, math/SU3GroupElement.java:494-505 */
+static void su3_proj(const double *e, double *v)
+{
+    double f[9];
+    f[0] = (2 * e[9] - e[13] - e[17]) / 3;
+    f[1] = (e[10] + e[12]) / 2;
+    f[2] = (e[11] + e[15]) / 2;
+    f[3] = (e[1] - e[3]) / 2;
+    f[4] = (2 * e[13] - e[17] - e[9]) / 3;
+    f[5] = (e[14] + e[16]) / 2;
+    f[6] = (e[2] - e[6]) / 2;
+    f[7] = (e[5] - e[7]) / 2;
+    f[8] = (2 * e[17] - e[9] - e[13]) / 3;
+    memcpy(v, f, sizeof(f));
+}
+
+/* SU3AlgebraElement hermiticize step shared by act and the log
+ * (math/SU3AlgebraElement.java:155-165) */
+static void su3_hermiticize(const double *values, double *f)
+{
+    f[0] = values[0];
+    f[4] = values[4];
+    f[8] = values[8];
+    f[1] = (values[1] + values[3]) / 2;
+    f[2] = (values[2] + values[6]) / 2;
+    f[5] = (values[5] + values[7]) / 2;
+    f[3] = (values[12] - values[10]) / 2;
+    f[6] = (values[15] - values[11]) / 2;
+    f[7] = (values[16] - values[14]) / 2;
+}
+
+/* SU3AlgebraElement.act, math/SU3AlgebraElement.java:144-168 */
+static void su3_act(const double *v, const double *a, double *out)
+{
+    double temp[18] = {v[0], v[1], v[2], v[1], v[4], v[5], v[2], v[5], v[8],
+                       0, -v[3], -v[6], v[3], 0, -v[7], v[6], v[7], 0};
+    double aadj[18], t1[18], t2[18], f[9];
+    su3_adj(a, aadj);
+    su3_mult(temp, aadj, t1);
+    su3_mult(a, t1, t2);
+    su3_hermiticize(t2, f);
+    memcpy(out, f, sizeof(f));
+}
+
+/* SU3AlgebraElement.square, math/SU3AlgebraElement.java:174-176 */
+static double su3_square(const double *v)
+{
+    return 2 * (v[0] * v[0] + v[4] * v[4] + v[8] * v[8] +
+                 2 * (v[1] * v[1] + v[2] * v[2] + v[3] * v[3] + v[5] * v[5] + v[6] * v[6] +
+                      v[7] * v[7]));
+}
+
+static int su3_normalize(double *vec)
+{
+    double norm = 0;
+    for (int i = 0; i < 6; i++) norm += vec[i] * vec[i];
+    norm = sqrt(norm);
+    if (fabs(norm) < 1.E-12) return 0;
+    for (int i = 0; i < 6; i++) vec[i] /= norm;
+    return 1;
+}
+
+/* SU3AlgebraElement.groupElementTaylorSeries, math/SU3AlgebraElement.java:389-400 */
+static void su3_getlink_taylor(const double *v, int iterations, double *out)
+{
+    double result[18] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double inter[18] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double mult[18] = {0, v[3], v[6], -v[3], 0, v[7], -v[6], -v[7], 0,
+                       v[0], v[1], v[2], v[1], v[4], v[5], v[2], v[5], v[8]};
+    for (int i = 1; i <= iterations; i++) {
+        double t[18];
+        su3_mult(inter, mult, t);
+        double s = 1.0 / i;
+        for (int k = 0; k < 18; k++) inter[k] = t[k] * s;
+        for (int k = 0; k < 18; k++) result[k] = result[k] + inter[k];
+    }
+    memcpy(out, result, sizeof(result));
+}
+
+/* SU3AlgebraElement.groupElementDecompositionMethod + getLink,
+ * math/SU3AlgebraElement.java:240-417.  Returns 0 if the Taylor branch must be
+ * used with *iters iterations. */
+static int su3_getlink_decomp(const double *v, double *out, int *iters)
+{
+    double trSq = su3_square(v) / 2;
+    if (trSq <= 1.E-0) { *iters = 15; return 0; }
+    double det = -v[2] * v[2] * v[4] + v[6] * (2 * v[3] * v[5] - v[4] * v[6] + 2 * v[1] * v[7]) +
+                 2 * v[2] * (v[1] * v[5] - v[3] * v[7]) - (v[1] * v[1] + v[3] * v[3]) * v[8] -
+                 v[0] * (v[5] * v[5] + v[7] * v[7] - v[4] * v[8]);
+    double linTerm = -trSq / 2;
+    double preRad = det * det + pow(linTerm, 3) * 4 / 27;
+    if (preRad > 0) preRad = 0;
+    double radIm = sqrt(-preRad);
+    double preOmegaRe = det / 2, preOmegaIm = radIm / 2;
+    double th = atan2(preOmegaIm, preOmegaRe);
+    double r = pow(preOmegaRe * preOmegaRe + preOmegaIm * preOmegaIm, 1. / 6);
+    double ths[3], ph[3];
+    for (int i = 0; i < 3; i++) ths[i] = (th + 2 * M_PI * i) / 3;
+    for (int i = 0; i < 3; i++) {
+        if (fabs(r) == 0)
+            ph[i] = 0;
+        else
+            ph[i] = r * cos(ths[i]) - (linTerm * cos(ths[i])) / (3 * r);
+    }
+    const double dc = 1.E-2;
+    if (fabs(1 - ph[0] / ph[1]) < dc || fabs(1 - ph[0] / ph[2]) < dc ||
+        fabs(1 - ph[1] / ph[2]) < dc) {
+        *iters = 25;
+        return 0;
+    }
+    double vec[3][6];
+    for (int i = 0; i < 3; i++) {
+        double opp = ph[(i + 1) % 3] * ph[(i + 2) % 3];
+        double ops = ph[0] + ph[1] + ph[2] - ph[i];
+        double *w = vec[i];
+        w[0] = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3] + v[6] * v[6] + opp - v[0] * ops;
+        w[1] = v[2] * v[5] + v[6] * v[7] + v[1] * (v[0] + v[4] - ops);
+        w[2] = v[1] * v[5] - v[3] * v[7] + v[2] * (v[0] + v[8] - ops);
+        w[3] = 0;
+        w[4] = v[5] * v[6] - v[2] * v[7] + v[3] * (v[0] + v[4] - ops);
+        w[5] = v[3] * v[5] + v[1] * v[7] + v[6] * (v[0] + v[8] - ops);
+        if (!su3_normalize(w)) {
+            w[0] = v[2] * v[5] + v[6] * v[7] + v[1] * (v[0] + v[4] - ops);
+            w[1] = v[1] * v[1] + v[3] * v[3] + v[4] * v[4] + v[5] * v[5] + v[7] * v[7] + opp - v[4] * ops;
+            w[2] = v[1] * v[2] + v[3] * v[6] + v[5] * (v[4] + v[8] - ops);
+            w[3] = v[2] * v[7] - v[5] * v[6] - v[3] * (v[0] + v[4] - ops);
+            w[4] = 0;
+            w[5] = v[1] * v[6] - v[2] * v[3] + v[7] * (v[4] + v[8] - ops);
+            if (!su3_normalize(w)) {
+                w[0] = v[1] * v[5] - v[3] * v[7] + v[2] * (v[0] + v[8] - ops);
+                w[1] = v[1] * v[2] + v[3] * v[6] + v[5] * (v[4] + v[8] - ops);
+                w[2] = v[2] * v[2] + v[5] * v[5] + v[6] * v[6] + v[7] * v[7] + v[8] * v[8] + opp - v[8] * ops;
+                w[3] = -v[3] * v[5] - v[1] * v[7] - v[6] * (v[0] + v[8] - ops);
+                w[4] = -v[1] * v[6] + v[2] * v[3] - v[7] * (v[4] + v[8] - ops);
+                w[5] = 0;
+                if (!su3_normalize(w)) {
+                    for (int j = 0; j < 6; j++) w[j] = 0;
+                    w[i] = 1;
+                }
+            }
+        }
+    }
+    double unit[18] = {vec[0][0], vec[1][0], vec[2][0], vec[0][1], vec[1][1], vec[2][1],
+                       vec[0][2], vec[1][2], vec[2][2], vec[0][3], vec[1][3], vec[2][3],
+                       vec[0][4], vec[1][4], vec[2][4], vec[0][5], vec[1][5], vec[2][5]};
+    double diag[18] = {cos(ph[0]), 0, 0, 0, cos(ph[1]), 0, 0, 0, cos(ph[2]),
+                       sin(ph[0]), 0, 0, 0, sin(ph[1]), 0, 0, 0, sin(ph[2])};
+    double t1[18], ua[18];
+    su3_mult(unit, diag, t1);
+    su3_adj(unit, ua);
+    su3_mult(t1, ua, out);
+    return 1;
+}
+
+static void su3_getlink(const double *v, double *out)
+{
+    int iters = 15;
+    if (!su3_getlink_decomp(v, out, &iters)) su3_getlink_taylor(v, iters, out);
+}
+
+/* SU3AlgebraElement.get(j), math/SU3AlgebraElement.java:117-129 */
+static void su3_to_gen(const double *v, double *g)
+{
+    double s3 = sqrt(3);
+    g[0] = 2 * v[1];
+    g[1] = 2 * v[3];
+    g[2] = v[0] - v[4];
+    g[3] = 2 * v[2];
+    g[4] = 2 * v[6];
+    g[5] = 2 * v[5];
+    g[6] = 2 * v[7];
+    g[7] = (v[0] + v[4] - 2 * v[8]) / s3;
+}
+
+/* SU3AlgebraElement(double[8]) -> set(j, value) for j=0..7 from zero,
+ * math/SU3AlgebraElement.java:36-49, 93-115 */
+static void su3_from_gen(const double *gen, double *v)
+{
+    double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < 8; j++) {
+        double g[8];
+        su3_to_gen(w, g);
+        double diff = (gen[j] - g[j]) / 2;
+        switch (j) {
+        case 0: w[1] += diff; break;
+        case 1: w[3] += diff; break;
+        case 2: w[0] += diff; w[4] -= diff; break;
+        case 3: w[2] += diff; break;
+        case 4: w[6] += diff; break;
+        case 5: w[5] += diff; break;
+        case 6: w[7] += diff; break;
+        case 7:
+            w[0] += diff / sqrt(3);
+            w[4] += diff / sqrt(3);
+            w[8] -= 2 * diff / sqrt(3);
+            break;
+        }
+    }
+    memcpy(v, w, sizeof(w));
+}
+
+/* ---- generic dispatch ---- */
+void orc_group_mult(int nc, const double *l, const double *r, double *out)
+{
+    if (nc == 3) su3_mult(l, r, out); else su2_mult(l, r, out);
+}
+void orc_group_adj(int nc, const double *u, double *out)
+{
+    if (nc == 3) { su3_adj(u, out); return; }
+    out[0] = u[0]; out[1] = -u[1]; out[2] = -u[2]; out[3] = -u[3];
+}
+void orc_group_proj(int nc, const double *u, double *alg)
+{
+    if (nc == 3) { su3_proj(u, alg); return; }
+    /* SU2GroupElement.proj, math/SU2GroupElement.java:254-263 */
+    alg[0] = 2 * u[1]; alg[1] = 2 * u[2]; alg[2] = 2 * u[3];
+}
+void orc_alg_getlink(int nc, const double *alg, double *u)
+{
+    if (nc == 3) su3_getlink(alg, u); else su2_getlink(alg, u);
+}
+void orc_alg_act(int nc, const double *alg, const double *g, double *out)
+{
+    if (nc == 3) su3_act(alg, g, out); else su2_act(alg, g, out);
+}
+double orc_alg_square(int nc, const double *alg)
+{
+    if (nc == 3) return su3_square(alg);
+    return alg[0] * alg[0] + alg[1] * alg[1] + alg[2] * alg[2];
+}
+void orc_alg_to_gen(int nc, const double *alg, double *gen)
+{
+    if (nc == 3) { su3_to_gen(alg, gen); return; }
+    gen[0] = alg[0]; gen[1] = alg[1]; gen[2] = alg[2];
+}
+void orc_gen_to_alg(int nc, const double *gen, double *alg)
+{
+    if (nc == 3) { su3_from_gen(gen, alg); return; }
+    alg[0] = gen[0]; alg[1] = gen[1]; alg[2] = gen[2];
+}
+
+/* Bilinear form 2 tr(XY) in the algebra layout (the polarisation of square()). */
+static double alg_dot(int nc, const double *x, const double *y)
+{
+    if (nc == 3)
+        return 2 * (x[0] * y[0] + x[4] * y[4] + x[8] * y[8] +
+                    2 * (x[1] * y[1] + x[2] * y[2] + x[3] * y[3] + x[5] * y[5] + x[6] * y[6] +
+                         x[7] * y[7]));
+    return x[0] * y[0] + x[1] * y[1] + x[2] * y[2];
+}
+
+/* ------------------------------------------------------------------------- */
+/* Grid (physics/grid/Grid.java)                                              */
+/* ------------------------------------------------------------------------- */
+static long vol(const orc_params *p) { return (long)p->n[0] * p->n[1] * p->n[2]; }
+
+/* Grid.shift, physics/grid/Grid.java:802-823 (cummulatedCellCount :534-538) */
+long orc_shift(const orc_params *p, long index, int direction, int orientation)
+{
+    long ccc[4];
+    ccc[3] = 1;
+    for (int i = 2; i >= 0; i--) ccc[i] = ccc[i + 1] * p->n[i];
+    long result = index;
+    long directionIndex = index / ccc[direction + 1];
+    long within = directionIndex % p->n[direction];
+    if (orientation > 0) {
+        if (within == p->n[direction] - 1) result -= ccc[direction];
+        result += ccc[direction + 1];
+    } else if (orientation < 0) {
+        if (within == 0) result += ccc[direction];
+        result -= ccc[direction + 1];
+    }
+    return result;
+}
+
+static inline const double *link(const orc_params *p, const double *U, long index, int dir)
+{
+    return U + ((size_t)index * 3 + dir) * orc_ng(p->nc);
+}
+
+/* Grid.getLink, physics/grid/Grid.java:712-727 */
+static void get_link(const orc_params *p, const double *U, long index, int dir, int orient,
+                     double *out)
+{
+    int ng = orc_ng(p->nc);
+    if (orient < 0)
+        orc_group_adj(p->nc, link(p, U, orc_shift(p, index, dir, orient), dir), out);
+    else
+        memcpy(out, link(p, U, index, dir), sizeof(double) * ng);
+}
+
+static void group_identity(int nc, double *u)
+{
+    int ng = orc_ng(nc);
+    memset(u, 0, sizeof(double) * ng);
+    if (nc == 3) { u[0] = u[4] = u[8] = 1; } else u[0] = 1;
+}
+
+/* Grid.getStapleSum, physics/grid/Grid.java:675-696 */
+void orc_staple_sum(const orc_params *p, const double *U, long index, int d, double *S)
+{
+    int nc = p->nc, ng = orc_ng(nc);
+    double U1[NG_MAX], U2[NG_MAX], t[NG_MAX], adj[NG_MAX];
+    memset(S, 0, sizeof(double) * ng);
+    long ci1 = orc_shift(p, index, d, 1);
+    for (int i = 0; i < 3; i++) {
+        if (i == d) continue;
+        long ci2 = orc_shift(p, index, i, 1);
+        long ci3 = orc_shift(p, ci1, i, -1);
+        long ci4 = orc_shift(p, index, i, -1);
+        orc_group_adj(nc, link(p, U, ci2, d), adj);
+        orc_group_mult(nc, link(p, U, ci1, i), adj, U1);
+        orc_group_adj(nc, link(p, U, index, i), adj);
+        orc_group_mult(nc, U1, adj, t);
+        memcpy(U1, t, sizeof(double) * ng);
+        orc_group_mult(nc, link(p, U, ci4, d), link(p, U, ci3, i), U2);
+        orc_group_adj(nc, U2, t);
+        orc_group_mult(nc, t, link(p, U, ci4, i), U2);
+        double areaFactor = 1.0 / pow(p->a[i], 2);
+        for (int k = 0; k < ng; k++) U1[k] = U1[k] + U2[k];
+        for (int k = 0; k < ng; k++) U1[k] = U1[k] * areaFactor;
+        for (int k = 0; k < ng; k++) S[k] = S[k] + U1[k];
+    }
+}
+
+/* Grid.getPlaquette, physics/grid/Grid.java:609-642 */
+void orc_plaquette(const orc_params *p, const double *U, long index, int d1, int d2, int o1,
+                   int o2, double *out)
+{
+    int nc = p->nc, ng = orc_ng(nc);
+    long x1 = index;
+    long x2 = orc_shift(p, x1, d1, o1);
+    long x3 = orc_shift(p, x2, d2, o2);
+    long x4 = orc_shift(p, x3, d1, -o1);
+    double L[4][NG_MAX], A[NG_MAX], T[NG_MAX];
+    get_link(p, U, x1, d1, o1, L[0]);
+    get_link(p, U, x2, d2, o2, L[1]);
+    get_link(p, U, x3, d1, -o1, L[2]);
+    get_link(p, U, x4, d2, -o2, L[3]);
+    group_identity(nc, A);
+    for (int k = 0; k < 4; k++) {
+        orc_group_mult(nc, A, L[k], T);
+        memcpy(A, T, sizeof(double) * ng);
+    }
+    memcpy(out, A, sizeof(double) * ng);
+}
+
+/* Grid.getB, physics/grid/Grid.java:901-920 */
+void orc_get_b(const orc_params *p, const double *U, long index, int dir, double *alg)
+{
+    int j = 0, k = 0, na = orc_na(p->nc);
+    switch (dir) {
+    case 0: j = 1; k = 2; break;
+    case 1: j = 2; k = 0; break;
+    case 2: j = 0; k = 1; break;
+    }
+    double P[NG_MAX];
+    orc_plaquette(p, U, index, j, k, 1, 1, P);
+    orc_group_proj(p->nc, P, alg);
+    double f = p->a[dir] / (p->a[j] * p->a[k]);
+    for (int c = 0; c < na; c++) alg[c] = alg[c] * f;
+}
+
+/* Grid.getGaussConstraint, physics/grid/Grid.java:944-968 */
+void orc_gauss_constraint(const orc_params *p, const double *U, const double *E,
+                          const double *rho, long index, double *alg)
+{
+    int nc = p->nc, na = orc_na(nc);
+    double gauss[NA_MAX] = {0}, e[NA_MAX], g[NG_MAX];
+    for (int i = 0; i < 3; i++) {
+        double unitFactor = p->g * p->a[i];
+        long sh = orc_shift(p, index, i, -1);
+        get_link(p, U, index, i, -1, g);
+        orc_alg_act(nc, E + ((size_t)sh * 3 + i) * na, g, e);
+        for (int c = 0; c < na; c++) e[c] = e[c] * -1.0;
+        for (int c = 0; c < na; c++) e[c] = e[c] + E[((size_t)index * 3 + i) * na + c];
+        double f = 1.0 / (p->a[i] * unitFactor);
+        for (int c = 0; c < na; c++) e[c] = e[c] * f;
+        for (int c = 0; c < na; c++) gauss[c] = gauss[c] + e[c];
+    }
+    for (int c = 0; c < na; c++) alg[c] = gauss[c] - rho[(size_t)index * na + c];
+}
+
+/* ------------------------------------------------------------------------- */
+/* FastTYMSolver (physics/fields/FastTYMSolver.java)                          */
+/* ------------------------------------------------------------------------- */
+
+/* CombinedUpdate.execute, physics/fields/FastTYMSolver.java:50-62 (the unit
+ * factor -g*a_i*dt is set in step(), :25-32) */
+static void combined_update_site(const orc_params *p, const double *U, double *E,
+                                 const double *J, double *Unext, long index)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    double S[NG_MAX], temp[NG_MAX], pr[NA_MAX], ve[NA_MAX], V[NG_MAX], t[NG_MAX];
+    for (int i = 0; i < 3; i++) {
+        double unitFactor = -(p->g * p->a[i]) * p->dt;
+        const double *Ui = link(p, U, index, i);
+        double *Ei = E + ((size_t)index * 3 + i) * na;
+        const double *Ji = J + ((size_t)index * 3 + i) * na;
+        orc_staple_sum(p, U, index, i, S);
+        orc_group_mult(nc, Ui, S, temp);
+        orc_group_proj(nc, temp, pr);
+        for (int c = 0; c < na; c++) Ei[c] = Ei[c] + pr[c] * p->dt;
+        for (int c = 0; c < na; c++) Ei[c] = Ei[c] + Ji[c] * unitFactor;
+        for (int c = 0; c < na; c++) ve[c] = Ei[c] * -p->dt;
+        orc_alg_getlink(nc, ve, V);
+        orc_group_mult(nc, V, Ui, t);
+        memcpy(Unext + ((size_t)index * 3 + i) * ng, t, sizeof(double) * ng);
+    }
+}
+
+void orc_update_grid(const orc_params *p, const double *U, double *E, const double *J,
+                     double *Unext, const uint8_t *active)
+{
+    long V = vol(p);
+    for (long x = 0; x < V; x++)
+        if (!active || active[x]) combined_update_site(p, U, E, J, Unext, x);
+}
+
+void orc_update_grid_omp(const orc_params *p, const double *U, double *E, const double *J,
+                         double *Unext, const uint8_t *active, int nthreads)
+{
+    long V = vol(p);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (long x = 0; x < V; x++)
+        if (!active || active[x]) combined_update_site(p, U, E, J, Unext, x);
+    (void)nthreads;
+}
+
+int orc_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* UpdateLinks.execute, physics/fields/FastTYMSolver.java:73-83 */
+void orc_update_links(const orc_params *p, const double *U, const double *E, double *Unext,
+                      const uint8_t *active)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    long Vn = vol(p);
+    for (long x = 0; x < Vn; x++) {
+        if (active && !active[x]) continue;
+        for (int k = 0; k < 3; k++) {
+            double ve[NA_MAX], V[NG_MAX], t[NG_MAX];
+            const double *Ek = E + ((size_t)x * 3 + k) * na;
+            for (int c = 0; c < na; c++) ve[c] = Ek[c] * -p->dt;
+            orc_alg_getlink(nc, ve, V);
+            orc_group_mult(nc, V, link(p, U, x, k), t);
+            memcpy(Unext + ((size_t)x * 3 + k) * ng, t, sizeof(double) * ng);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Reductions                                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* FieldMeasurements EFieldSquared/BFieldSquared/GaussLaw/TotalChargeSquared
+ * (physics/measurements/FieldMeasurements.java:68-231) combined as
+ * BulkQuantitiesInTime.calculate does (diagnostics/methods/BulkQuantitiesInTime.java:83-121) */
+void orc_bulk(const orc_params *p, const double *U, const double *Unext, const double *E,
+              const double *rho, const uint8_t *eval, double *out)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    double ev[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, gsum = 0.0, charge = 0.0;
+    double uf[3];
+    for (int i = 0; i < 3; i++) uf[i] = pow(p->g * p->a[i], -2);
+    for (long x = 0; x < V; x++) {
+        if (eval && !eval[x]) continue;
+        double b0[NA_MAX], b1[NA_MAX], gg[NA_MAX];
+        for (int i = 0; i < 3; i++) {
+            double r = 0.0;
+            r += orc_alg_square(nc, E + ((size_t)x * 3 + i) * na) * uf[i];
+            ev[i] += r;
+        }
+        for (int i = 0; i < 3; i++) {
+            orc_get_b(p, U, x, i, b0);
+            orc_get_b(p, Unext, x, i, b1);
+            double r = 0.0;
+            r += 0.5 * (orc_alg_square(nc, b0) + orc_alg_square(nc, b1)) * uf[i];
+            bv[i] += r;
+        }
+        orc_gauss_constraint(p, U, E, rho, x, gg);
+        gsum += orc_alg_square(nc, gg);
+        charge += orc_alg_square(nc, rho + (size_t)x * na);
+    }
+    double es[3], bs[3];
+    for (int i = 0; i < 3; i++) { es[i] = ev[i] / V; bs[i] = bv[i] / V; }
+    out[0] = es[0]; out[1] = es[1]; out[2] = es[2];
+    out[3] = bs[0]; out[4] = bs[1]; out[5] = bs[2];
+    out[6] = -es[0] + es[1] + es[2] - bs[0] + bs[1] + bs[2];
+    out[7] = +es[0] - es[1] + es[2] + bs[0] - bs[1] + bs[2];
+    out[8] = +es[0] + es[1] - es[2] + bs[0] + bs[1] - bs[2];
+    out[9] = gsum / V;
+    out[10] = sqrt(charge) / V;
+    out[11] = es[0] + es[1] + es[2];
+    out[12] = bs[0] + bs[1] + bs[2];
+}
+
+/* EnergyDensity.ComponentComputation, diagnostics/methods/EnergyDensity.java:119-166.
+ * Kept as in the reference: the unit factor of direction 0 for every d, and B
+ * summed over U and Unext before squaring. */
+void orc_energy_density(const orc_params *p, const double *U, const double *Unext,
+                        const double *E, const uint8_t *eval, double *out)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    double uf = pow(p->g * p->a[0], -2);
+    for (long x = 0; x < V; x++) {
+        out[x] = 0.0;
+        if (eval && !eval[x]) continue;
+        for (int d = 0; d < 3; d++) {
+            double b0[NA_MAX], b1[NA_MAX];
+            orc_get_b(p, U, x, d, b0);
+            orc_get_b(p, Unext, x, d, b1);
+            for (int c = 0; c < na; c++) b0[c] = b0[c] + b1[c];
+            double Esq = 0.5 * orc_alg_square(nc, E + ((size_t)x * 3 + d) * na);
+            double Bsq = 0.25 * orc_alg_square(nc, b0);
+            out[x] += (Esq + Bsq) * uf;
+        }
+    }
+}
+
+static void cell_pos(const orc_params *p, long index, int *pos)
+{
+    for (int i = 2; i >= 0; i--) {
+        pos[i] = (int)(index % p->n[i]);
+        index -= pos[i];
+        index /= p->n[i];
+    }
+}
+
+/* ProjectedEnergyDensity.EnergyDensityComputation,
+ * diagnostics/methods/ProjectedEnergyDensity.java:114-179 */
+void orc_projected_energy(const orc_params *p, const double *U, const double *Unext,
+                          const double *E, const uint8_t *eval, int dir, double *out)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    int N = p->n[dir];
+    double *T_el = out, *T_mag = out + N, *L_el = out + 2 * N, *L_mag = out + 3 * N;
+    for (int i = 0; i < 4 * N; i++) out[i] = 0.0;
+    double areaFactor = V / ((double)N);
+    double uf[3];
+    for (int i = 0; i < 3; i++) uf[i] = pow(p->g * p->a[i], -2) / areaFactor;
+    for (long x = 0; x < V; x++) {
+        if (eval && !eval[x]) continue;
+        int pos[3];
+        cell_pos(p, x, pos);
+        int pi = pos[dir];
+        double eTel = 0.0, eLel = 0.0, eTmag = 0.0, eLmag = 0.0;
+        for (int j = 0; j < 3; j++) {
+            double b0[NA_MAX], b1[NA_MAX];
+            double electric = 0.5 * orc_alg_square(nc, E + ((size_t)x * 3 + j) * na) * uf[j];
+            orc_get_b(p, U, x, j, b0);
+            orc_get_b(p, Unext, x, j, b1);
+            double magnetic = 0.25 * (orc_alg_square(nc, b0) + orc_alg_square(nc, b1)) * uf[j];
+            if (j == dir) { eLel += electric; eLmag += magnetic; }
+            else { eTel += electric; eTmag += magnetic; }
+        }
+        T_el[pi] += eTel;
+        T_mag[pi] += eTmag;
+        L_el[pi] += eLel;
+        L_mag[pi] += eLmag;
+    }
+}
+
+void orc_gauss_field(const orc_params *p, const double *U, const double *E, const double *rho,
+                     double *out)
+{
+    int na = orc_na(p->nc);
+    long V = vol(p);
+    for (long x = 0; x < V; x++) orc_gauss_constraint(p, U, E, rho, x, out + (size_t)x * na);
+}
+
+/* ------------------------------------------------------------------------- */
+/* CPIC NGP                                                                   */
+/* ------------------------------------------------------------------------- */
+
+/* GridFunctions.nearestGridPoint, physics/util/GridFunctions.java:67-73 ((int) Math.rint) */
+void orc_ngp(const orc_params *p, const double *pos, int32_t *c)
+{
+    for (int i = 0; i < 3; i++) c[i] = (int32_t)rint(pos[i] / p->a[i]);
+}
+
+/* Grid.getCellIndex + periodic, physics/grid/Grid.java:757-786 */
+static long cell_index(const orc_params *p, const int32_t *c)
+{
+    long idx = 0;
+    for (int i = 0; i < 3; i++) {
+        long r = ((long)c[i] % p->n[i] + p->n[i]) % p->n[i];
+        idx = i == 0 ? r : idx * p->n[i] + r;
+    }
+    return idx;
+}
+
+/* YangMillsParticle.reassignValues, physics/particles/YangMillsParticle.java:117-125 */
+void orc_cpic_reassign(int nc, long np, double *pos0, double *pos1, double *Q0, double *Q1)
+{
+    int na = orc_na(nc);
+    for (long k = 0; k < np; k++) {
+        for (int i = 0; i < 3; i++) {
+            double t = pos0[k * 3 + i]; pos0[k * 3 + i] = pos1[k * 3 + i]; pos1[k * 3 + i] = t;
+        }
+        for (int c = 0; c < na; c++) {
+            double t = Q0[k * na + c]; Q0[k * na + c] = Q1[k * na + c]; Q1[k * na + c] = t;
+        }
+    }
+}
+
+/* CGCParticleInterpolationNGP.interpolateChargedensity, physics/grid/CGCParticleInterpolationNGP.java:52-68 */
+void orc_cpic_charge_density(const orc_params *p, long np, const double *pos0, const double *Q0,
+                             double *rho)
+{
+    int na = orc_na(p->nc);
+    for (long k = 0; k < np; k++) {
+        int32_t c[3];
+        orc_ngp(p, pos0 + k * 3, c);
+        long ci = cell_index(p, c);
+        for (int m = 0; m < na; m++) rho[ci * na + m] = rho[ci * na + m] + Q0[k * na + m];
+    }
+}
+
+/* CGCParticleSolver.updatePosition, physics/movement/solver/CGCParticleSolver.java:15-21;
+ * AbsorbingParticleBoundaryConditions.applyOnParticle is a no-op (:31-40). */
+void orc_cpic_update_positions(const orc_params *p, long np, const double *pos0, double *pos1,
+                               const double *vel)
+{
+    for (long k = 0; k < np; k++)
+        for (int i = 0; i < 3; i++) pos1[k * 3 + i] = pos0[k * 3 + i] + vel[k * 3 + i] * p->dt;
+}
+
+/* CGCParticleInterpolationNGP.interpolateToParticle, :70-104 */
+void orc_cpic_to_particle(const orc_params *p, long np, const double *pos0, const double *pos1,
+                          const double *vel, const int32_t *dir, const double *Unext,
+                          double *Ulink, uint8_t *flag)
+{
+    int nc = p->nc, ng = orc_ng(nc);
+    for (long k = 0; k < np; k++) {
+        int32_t o[3], n[3];
+        int d = dir[k];
+        orc_ngp(p, pos0 + k * 3, o);
+        orc_ngp(p, pos1 + k * 3, n);
+        if (o[d] == n[d]) continue;
+        long co = cell_index(p, o), cn = cell_index(p, n);
+        if (vel[k * 3 + d] > 0)
+            memcpy(Ulink + k * ng, link(p, Unext, co, d), sizeof(double) * ng);
+        else
+            orc_group_adj(nc, link(p, Unext, cn, d), Ulink + k * ng);
+        flag[k] = 1;
+    }
+}
+
+/* CGCParticleSolver.updateCharge, physics/movement/solver/CGCParticleSolver.java:24-36 */
+void orc_cpic_update_charges(int nc, long np, double *Q0, double *Q1, const double *Ulink,
+                             uint8_t *flag)
+{
+    int na = orc_na(nc), ng = orc_ng(nc);
+    for (long k = 0; k < np; k++) {
+        if (flag[k]) {
+            double ua[NG_MAX];
+            orc_group_adj(nc, Ulink + k * ng, ua);
+            orc_alg_act(nc, Q0 + k * na, ua, Q1 + k * na);
+            flag[k] = 0;
+        } else {
+            for (int c = 0; c < na; c++) {
+                double t = Q1[k * na + c]; Q1[k * na + c] = Q0[k * na + c]; Q0[k * na + c] = t;
+            }
+        }
+    }
+}
+
+/* CGCParticleInterpolationNGP.interpolateToGrid, :15-50 */
+void orc_cpic_to_grid(const orc_params *p, long np, const double *pos0, const double *pos1,
+                      const double *vel, const int32_t *dir, const double *Q0, const double *Q1,
+                      double *J)
+{
+    int na = orc_na(p->nc);
+    double at = p->dt;
+    for (long k = 0; k < np; k++) {
+        int32_t o[3], n[3];
+        int d = dir[k];
+        orc_ngp(p, pos0 + k * 3, o);
+        orc_ngp(p, pos1 + k * 3, n);
+        if (o[d] == n[d]) continue;
+        long co = cell_index(p, o), cn = cell_index(p, n);
+        if (vel[k * 3 + d] > 0) {
+            double f = p->a[d] / at;
+            double *Jd = J + ((size_t)co * 3 + d) * na;
+            for (int c = 0; c < na; c++) Jd[c] = Jd[c] + Q0[k * na + c] * f;
+        } else {
+            double f = -p->a[d] / at;
+            double *Jd = J + ((size_t)cn * 3 + d) * na;
+            for (int c = 0; c < na; c++) Jd[c] = Jd[c] + Q1[k * na + c] * f;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Seeded synthetic initial conditions                                        */
+/* ------------------------------------------------------------------------- */
+
+/* Counter-based generator: splitmix64 finaliser of (seed, counter); two 53-bit
+ * uniforms per normal (Box-Muller, cosine branch).  The same integer recipe is
+ * used by the GPU initial-condition kernels. */
+static inline uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static inline double unif(uint64_t seed, uint64_t ctr)
+{
+    uint64_t h = mix64(seed ^ mix64(ctr));
+    return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+double orc_normal(uint64_t seed, uint64_t ctr)
+{
+    double u1 = unif(seed, 2 * ctr), u2 = unif(seed, 2 * ctr + 1);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+void orc_random_gen(uint64_t seed, uint64_t stream, long count, double sigma, double *out)
+{
+    uint64_t base = stream << 40;
+    for (long k = 0; k < count; k++) out[k] = sigma * orc_normal(seed, base + (uint64_t)k);
+}
+
+/* div E (x) = sum_i c_i [E_i(x) - Ad(U_i(x-i)^dagger) E_i(x-i)], c_i = 1/(a_i g a_i):
+ * the E part of Grid.getGaussConstraint (Grid.java:944-968). */
+static void op_div(const orc_params *p, const double *U, const double *E, double *out)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    for (long x = 0; x < V; x++) {
+        double acc[NA_MAX] = {0}, e[NA_MAX], g[NG_MAX];
+        for (int i = 0; i < 3; i++) {
+            double ci = 1.0 / (p->a[i] * p->g * p->a[i]);
+            long sh = orc_shift(p, x, i, -1);
+            orc_group_adj(nc, link(p, U, sh, i), g);
+            orc_alg_act(nc, E + ((size_t)sh * 3 + i) * na, g, e);
+            for (int c = 0; c < na; c++)
+                acc[c] += ci * (E[((size_t)x * 3 + i) * na + c] - e[c]);
+        }
+        memcpy(out + (size_t)x * na, acc, sizeof(double) * na);
+    }
+}
+/* The adjoint of op_div: (divT l)_i(x) = c_i [l(x) - Ad(U_i(x)) l(x+i)]. */
+static void op_divT(const orc_params *p, const double *U, const double *l, double *out)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    for (long x = 0; x < V; x++)
+        for (int i = 0; i < 3; i++) {
+            double ci = 1.0 / (p->a[i] * p->g * p->a[i]), e[NA_MAX];
+            long sh = orc_shift(p, x, i, 1);
+            orc_alg_act(nc, l + (size_t)sh * na, link(p, U, x, i), e);
+            for (int c = 0; c < na; c++)
+                out[((size_t)x * 3 + i) * na + c] = ci * (l[(size_t)x * na + c] - e[c]);
+        }
+}
+
+static double field_dot(int nc, long n, const double *x, const double *y)
+{
+    int na = orc_na(nc);
+    double s = 0.0;
+    for (long k = 0; k < n; k++) s += alg_dot(nc, x + k * na, y + k * na);
+    return s;
+}
+
+int orc_gauss_project_cg(const orc_params *p, const double *U, double *E, const double *rho,
+                         double tol_g2, int maxit, double *final_g2)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    size_t ns = (size_t)V * na, nl = ns * 3;
+    double *r = malloc(ns * sizeof(double)), *pp = malloc(ns * sizeof(double));
+    double *Ap = malloc(ns * sizeof(double)), *mu = calloc(ns, sizeof(double));
+    double *tl = malloc(nl * sizeof(double));
+    /* r = rho - div E */
+    op_div(p, U, E, r);
+    for (size_t k = 0; k < ns; k++) r[k] = rho[k] - r[k];
+    memcpy(pp, r, ns * sizeof(double));
+    double rr = field_dot(nc, V, r, r);
+    int it = 0;
+    while (it < maxit && rr / V > tol_g2 * 1e-4) {
+        op_divT(p, U, pp, tl);
+        op_div(p, U, tl, Ap);
+        double pAp = field_dot(nc, V, pp, Ap);
+        if (!(pAp > 0)) break;
+        double alpha = rr / pAp;
+        for (size_t k = 0; k < ns; k++) { mu[k] += alpha * pp[k]; r[k] -= alpha * Ap[k]; }
+        double rr2 = field_dot(nc, V, r, r);
+        double beta = rr2 / rr;
+        rr = rr2;
+        for (size_t k = 0; k < ns; k++) pp[k] = r[k] + beta * pp[k];
+        it++;
+    }
+    /* E <- E + divT mu */
+    op_divT(p, U, mu, tl);
+    for (size_t k = 0; k < nl; k++) E[k] += tl[k];
+    double g2 = 0.0;
+    for (long x = 0; x < V; x++) {
+        double gg[NA_MAX];
+        orc_gauss_constraint(p, U, E, rho, x, gg);
+        g2 += orc_alg_square(nc, gg);
+    }
+    if (final_g2) *final_g2 = g2 / V;
+    free(r); free(pp); free(Ap); free(mu); free(tl);
+    return it;
+}
+
+/* GaussConstraintRestoration.computeGaussViolation,
+ * diagnostics/methods/GaussConstraintRestoration.java:117-139 */
+static double restoration_violation(const orc_params *p, const double *U, const double *Unext,
+                                    const double *rho, double *gv)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    long V = vol(p);
+    double factor = 1.0 / (p->dt * p->a[0]);
+    double total = 0.0;
+    for (long i = 0; i < V; i++) {
+        double C[NG_MAX] = {0}, C1[NG_MAX], C2[NG_MAX], t[NG_MAX], pr[NA_MAX];
+        for (int j = 0; j < 3; j++) {
+            long k = orc_shift(p, i, j, -1);
+            orc_group_adj(nc, link(p, U, i, j), t);
+            orc_group_mult(nc, link(p, Unext, i, j), t, C1);
+            orc_group_adj(nc, link(p, U, k, j), t);
+            orc_group_mult(nc, t, link(p, Unext, k, j), C2);
+            for (int c = 0; c < ng; c++) C[c] = C[c] + (C1[c] - C2[c]);
+        }
+        for (int c = 0; c < ng; c++) gv[(size_t)i * ng + c] = C[c] * factor;
+        orc_group_proj(nc, gv + (size_t)i * ng, pr);
+        for (int c = 0; c < na; c++) pr[c] = pr[c] - rho[(size_t)i * na + c];
+        total += orc_alg_square(nc, pr);
+    }
+    return total / V;
+}
+
+/* GaussConstraintRestoration.applyCorrection, :146-163 */
+static void restoration_correct(const orc_params *p, const double *U, double *Unext, double *E,
+                                const double *gv, double gamma)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    long V = vol(p);
+    double factor2 = -0.5 * p->a[0] * gamma;
+    for (long i = 0; i < V; i++)
+        for (int j = 0; j < 3; j++) {
+            long k = orc_shift(p, i, j, 1);
+            double t[NG_MAX], C1[NG_MAX], ua[NG_MAX], pr[NA_MAX];
+            orc_group_mult(nc, link(p, U, i, j), gv + (size_t)k * ng, t);
+            orc_group_adj(nc, link(p, U, i, j), ua);
+            orc_group_mult(nc, t, ua, C1);
+            for (int c = 0; c < ng; c++) C1[c] = C1[c] - gv[(size_t)i * ng + c];
+            orc_group_proj(nc, C1, pr);
+            double *Ej = E + ((size_t)i * 3 + j) * na;
+            for (int c = 0; c < na; c++) Ej[c] = Ej[c] + pr[c] * factor2;
+        }
+    orc_update_links(p, U, E, Unext, NULL);
+}
+
+/* GaussConstraintRestoration.iterateRestorationAlgorithm, :78-110 */
+int orc_gauss_restoration(const orc_params *p, double *U, double *Unext, double *E,
+                          const double *rho, double gamma, int maxit, double absval,
+                          double *final_violation)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    long V = vol(p);
+    size_t nlg = (size_t)V * 3 * ng, nla = (size_t)V * 3 * na;
+    double *gv = malloc((size_t)V * ng * sizeof(double));
+    double *bE = malloc(nla * sizeof(double)), *bUn = malloc(nlg * sizeof(double));
+    double total = restoration_violation(p, U, Unext, rho, gv);
+    double old = total;
+    int i;
+    for (i = 0; i < maxit; i++) {
+        if (total < absval) break;
+        memcpy(bE, E, nla * sizeof(double));
+        memcpy(bUn, Unext, nlg * sizeof(double));
+        restoration_correct(p, U, Unext, E, gv, gamma);
+        total = restoration_violation(p, U, Unext, rho, gv);
+        if (old - total < 0) {
+            memcpy(E, bE, nla * sizeof(double));
+            memcpy(Unext, bUn, nlg * sizeof(double));
+            total = old;
+            break;
+        }
+        old = total;
+    }
+    if (final_violation) *final_violation = total;
+    free(gv); free(bE); free(bUn);
+    return i;
+}
