@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 leapfrog: link-updates/s and the fraction of the HBM
+roofline for the precision form of the Yang-Mills leapfrog (SU(3), 128^3
+periodic lattice, dt = 0.05, FP32 links and E with re-unitarisation every 10
+steps, FP64 compensated reductions), with the plain FP64 GPU path on the same
+lattice beside it.
+
+One step = storeFields + updateGrid over the whole lattice (3 * 128^3 link
+updates).  ``value`` is timed with CUDA events on the handle's own stream over
+K steps with the fields resident in HBM (inputs are larger than L2: the links
+alone are 453 MB).  ``e2e`` is the same metric through the public C ABI with
+host buffers: upload of the initial U and E from pinned memory, the K steps
+with the BulkQuantities reductions every 10 steps read back to the host, and
+the download of the final U and E, all inside the timed region.
+
+``--impl reference`` times the CPU implementation of the path: the reference
+(Java) cannot be built or run on this machine, so its FP64 restatement (the
+oracle, C + OpenMP over all host threads) stands in; every step updates a
+bounded slab of the same lattice.
+
+Multi-GPU: the path is one lattice per GPU; N ranks run N independent
+replicas (weak scaling), with a barrier and max-over-ranks timing.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: ncolors, dims, precision, reunit_every, dt, sigma (A and E), bytes per link update
+    "su3_fp32_128": dict(nc=3, dims=(128, 128, 128), prec="f32", reunit=10, dt=0.05, sigma=0.2, bpl=208,
+                         label="SU(3) pure Yang-Mills leapfrog, 128^3 periodic, dt=0.05, FP32 links/E, "
+                               "reunitarisation every 10 steps, FP64 compensated reductions"),
+    "su3_fp64_128": dict(nc=3, dims=(128, 128, 128), prec="f64", reunit=0, dt=0.05, sigma=0.2, bpl=416,
+                         label="SU(3) pure Yang-Mills leapfrog, 128^3 periodic, dt=0.05, FP64"),
+    "su2_fp64_32": dict(nc=2, dims=(32, 32, 32), prec="f64", reunit=0, dt=0.05, sigma=0.1, bpl=112,
+                        label="SU(2) pure Yang-Mills leapfrog, 32^3 periodic, dt=0.05, FP64"),
+    "su2_fp32_128": dict(nc=2, dims=(128, 128, 128), prec="f32", reunit=10, dt=0.05, sigma=0.1, bpl=56,
+                         label="SU(2) pure Yang-Mills leapfrog, 128^3 periodic, dt=0.05, FP32"),
+}
+SEED = 20261203
+METRIC = "link-updates/s"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self, backend):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64,
+                         device="cuda" if self.td.get_backend() == "nccl" else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_for(workload):
+    """DRAM bytes per launch of the leapfrog kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        v = d.get(workload)
+        if isinstance(v, dict):
+            return v.get("dram_bytes_per_launch")
+        return v
+    return None
+
+
+def make_handle(w, prec_name, device):
+    import openpixi_gb300 as opx
+    prec = opx.OPX_F32 if prec_name == "f32" else opx.OPX_F64
+    return opx.Handle(w["nc"], w["dims"], a=1.0, dt=w["dt"], g=1.0, precision=prec,
+                      reunit_every=w["reunit"] if prec_name == "f32" else 0, device=device)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(w, U_ref, E_ref, target_s=12.0):
+    """The oracle (FP64 restatement of the reference update, C + OpenMP) on a bounded
+    sample of the same lattice: whole-lattice steps, or a leading slab of sites when
+    one step would exceed the time budget."""
+    import oracle
+    g = oracle.OracleGrid(w["nc"], w["dims"], a=1.0, dt=w["dt"], g=1.0)
+    g.U[...] = U_ref
+    g.E[...] = E_ref
+    g.update_links()
+    nth = cpu_threads()
+    plane = w["dims"][1] * w["dims"][2]
+    t = time.perf_counter()
+    g.update_grid_range_omp(0, plane, nth)
+    per_plane = max(time.perf_counter() - t, 1e-6)
+    planes = int(max(1, min(w["dims"][0], target_s / per_plane)))
+    sites = planes * plane
+    t = time.perf_counter()
+    g.update_grid_range_omp(0, sites, nth)
+    el = time.perf_counter() - t
+    return {"value": 3.0 * sites / el, "unit": METRIC, "cores": nth, "kind": "port",
+            "sample": f"one leapfrog update of {planes} of {w['dims'][0]} x0-planes ({sites} sites, "
+                      f"{3 * sites} link updates) of the same lattice, FP64, {nth} OpenMP threads, {el:.2f} s"}
+
+
+def run_reference(args, w, wname):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    g = oracle.OracleGrid(w["nc"], w["dims"], a=1.0, dt=w["dt"], g=1.0)
+    g.random_fields(SEED, w["sigma"], w["sigma"])
+    g.update_links()
+    nth = cpu_threads()
+    plane = w["dims"][1] * w["dims"][2]
+    t = time.perf_counter()
+    g.update_grid_range_omp(0, plane, nth)
+    per_plane = max(time.perf_counter() - t, 1e-6)
+    budget = 150.0 / max(1, args.steps + args.warmup)  # whole run within a few minutes
+    planes = int(max(1, min(w["dims"][0], budget / per_plane)))
+    sites = planes * plane
+    for _ in range(args.warmup):
+        g.update_grid_range_omp(0, sites, nth)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        g.store_fields()
+        g.update_grid_range_omp(0, sites, nth)
+    el = time.perf_counter() - t
+    value = 3.0 * sites * args.steps / el
+    sample = (f"each step: one leapfrog update (FastTYMSolver.CombinedUpdate restated in C, FP64) of "
+              f"{planes} of {w['dims'][0]} x0-planes ({sites} sites) of the same lattice; "
+              f"{nth} OpenMP threads; the Java reference cannot run here (no JDK)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_for(w, wname),
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nth, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_for(w, wname):
+    return {"workload": wname, "description": w["label"], "lattice": list(w["dims"]), "ncolors": w["nc"],
+            "dt": w["dt"], "a": 1.0, "g": 1.0, "reunit_every": w["reunit"], "precision": w["prec"],
+            "initial_fields": f"seeded Gaussian A and E (sigma={w['sigma']}), E projected onto Gauss's law "
+                              f"in FP64 on the device",
+            "l2": "inputs larger than L2 (links alone exceed 129 MB)" if np.prod(w["dims"]) >= 64 ** 3
+            else "lattice fits in L2", "parallelism": "replicas (one lattice per GPU)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="su3_fp32_128", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w, args.workload)
+
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    rank, world, local = dist_env()
+    device = local
+    dist = Dist("nccl" if world > 1 else "gloo")
+    V = int(np.prod(w["dims"]))
+    links = 3 * V
+
+    # ---- set-up (untimed): seeded fields, Gauss projection in FP64, Unext
+    h = make_handle(w, w["prec"], device)
+    h.init_random(SEED + rank, w["sigma"], w["sigma"])
+    cg_it, g2 = h.gauss_project(1e-24 if w["prec"] == "f32" else 1e-26, 5000)
+    U_host = opx.PinnedArray((V, 3, h.ng))
+    E_host = opx.PinnedArray((V, 3, h.na_ref))
+    h.download(N.FIELD_U, out=U_host.array)
+    h.download(N.FIELD_E, out=E_host.array)
+    h.initialize()
+    o0 = h.reduce()
+    for _ in range(args.warmup):
+        h.step(1)
+    h.synchronize()
+
+    # ---- timed region: K steps, fields resident in HBM, CUDA events on the handle's stream
+    clocks = ClockSampler(device)
+    clocks.start()
+    l0 = h.kernel_launches
+    dist.barrier()
+    h.synchronize()
+    ms = h.time_steps(args.steps)
+    h.synchronize()
+    dist.barrier()
+    launches = h.kernel_launches - l0
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = world * links * args.steps / (ms_max / 1000.0)
+    o1 = h.reduce()
+    e0, e1 = o0.e2_total + o0.b2_total, o1.e2_total + o1.b2_total
+
+    # ---- roofline: the leapfrog kernel timed launch by launch (CUDA events around each launch)
+    h.set_profiling(True)
+    nprof = min(args.steps, 50)
+    h.step(nprof)
+    pms, pn = h.phase_times()
+    h.set_profiling(False)
+    t_launch = pms[N.PHASE_EOM] / max(pn[N.PHASE_EOM], 1) / 1000.0
+    peak, peak_kind = hbm_peak()
+    achieved = w["bpl"] * links / t_launch / 1e9
+    traffic = traffic_for(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_link": w["bpl"], "links_per_launch": links,
+                "kernel": "k_update_grid", "launch_ms": t_launch * 1000.0}
+
+    # ---- the plain FP64 GPU path on the same lattice (same initial fields)
+    fp64 = None
+    if w["prec"] == "f32":
+        h64 = make_handle(w, "f64", device)
+        h64.upload(N.FIELD_U, U_host.array)
+        h64.upload(N.FIELD_E, E_host.array)
+        h64.initialize()
+        h64.step(3)
+        n64 = max(5, min(args.steps, 20))
+        ms64 = h64.time_steps(n64)
+        v64 = links * n64 / (ms64 / 1000.0)
+        fp64 = {"value": v64 * world, "unit": METRIC, "steps": n64,
+                "fp32_over_fp64": value / (v64 * world)}
+        h64.close()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2 = make_handle(w, w["prec"], device)
+        he = (h2.ng + h2.na_ref) * 8 * links
+        dist.barrier()
+        t = time.perf_counter()
+        h2.upload(N.FIELD_U, U_host.array)
+        h2.upload(N.FIELD_E, E_host.array)
+        h2.initialize()
+        nred = 0
+        for k in range(args.steps):
+            h2.step(1)
+            if (k + 1) % 10 == 0:
+                h2.reduce()
+                nred += 1
+        h2.download(N.FIELD_U, out=U_host.array)
+        h2.download(N.FIELD_E, out=E_host.array)
+        el = time.perf_counter() - t
+        el = dist.max(el)
+        e2e = {"value": world * links * args.steps / el, "unit": METRIC,
+               "h2d_bytes_per_step": he / args.steps,
+               "d2h_bytes_per_step": (he + nred * 64) / args.steps,
+               "note": "initial U,E uploaded from pinned host memory and final U,E downloaded inside the "
+                       "timed region (bytes amortised over the steps); BulkQuantities read back every 10 steps"}
+        h2.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, U_host.array, E_host.array)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": w["prec"], "data": "synthetic",
+                "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64,
+                "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
+                "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

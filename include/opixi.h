@@ -1,0 +1,186 @@
+/*
+ * opixi.h -- C ABI of libopixi_gpu.so, the GB300 (sm_103a) implementation of
+ * OpenPixi's temporal-gauge Yang-Mills leapfrog, its CPIC (NGP) coupling and
+ * the energy / Gauss-law reductions.
+ *
+ * The reference is Java and has no native boundary.  Each entry point below
+ * names the Java method it stands in for (paths relative to
+ * pixi/src/main/java/org/openpixi/pixi/).  A Java drop-in (JNI or Panama FFM)
+ * binds these symbols one to one.
+ *
+ * Conventions
+ *  - Every function returns an int status: OPX_OK (0) or a negative OPX_ERR_*.
+ *    opx_last_error() gives the message of the last failure on a handle (or the
+ *    last failure of opx_create when called with NULL).  No C++ exception
+ *    crosses this boundary.
+ *  - Host buffers are caller-owned and copied; the library owns device memory.
+ *  - A handle is used by one host thread at a time; all work of a handle is
+ *    queued on its own CUDA stream.
+ *  - Host data are always doubles (the reference is FP64).  An OPX_F32 handle
+ *    stores links and fields in FP32 on the device and converts on transfer.
+ *  - Host layout OPX_LAYOUT_REF is the reference's per-cell layout:
+ *      U, Unext : [V][3][ng]  ng = 4  (SU(2) e0..e3, SU2GroupElement.java:3-14)
+ *                             ng = 18 (SU(3) 9 real then 9 imaginary parts,
+ *                                      SU3GroupElement.java:3-11)
+ *      E, J     : [V][3][na]  na = 3  (SU(2) v0..v2, SU2AlgebraElement.java)
+ *                             na = 9  (SU(3) hermitian entries v[9],
+ *                                      SU3AlgebraElement.java:3-11)
+ *      rho      : [V][na]
+ *    OPX_LAYOUT_GEN is the same but with E, J, rho given as generator
+ *    components (SU3AlgebraElement.get(a), :117-129): 3 (SU(2)) or 8 (SU(3)).
+ *    Site index = ((x0*N1)+x1)*N2+x2, dimension 0 slowest (Grid.java:757-770).
+ */
+#ifndef OPIXI_H
+#define OPIXI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OPX_OK 0
+#define OPX_ERR_INVALID (-1)     /* bad argument, size or handle */
+#define OPX_ERR_CUDA (-2)        /* CUDA runtime / launch failure */
+#define OPX_ERR_NOMEM (-3)       /* device or pinned allocation failed */
+#define OPX_ERR_NUMERIC (-4)     /* device status word: NaN/Inf or bound exceeded */
+#define OPX_ERR_UNSUPPORTED (-5) /* combination not provided (e.g. CPIC on FP32) */
+#define OPX_ERR_TIMEOUT (-6)     /* a bounded device wait gave up */
+
+#define OPX_F64 0
+#define OPX_F32 1
+
+#define OPX_FIELD_U 0
+#define OPX_FIELD_UNEXT 1
+#define OPX_FIELD_E 2
+#define OPX_FIELD_J 3
+#define OPX_FIELD_RHO 4
+
+#define OPX_LAYOUT_REF 0
+#define OPX_LAYOUT_GEN 1
+
+/* Phase indices of opx_phase_times (the PerformanceTimer laps of
+ * physics/Simulation.java:392-433, plus reductions and reunitarisation). */
+#define OPX_PHASE_EOM 0   /* storeFields + updateGrid (E and Unext) */
+#define OPX_PHASE_CPIC 1  /* CIN+PUP+PIN+CUP+JIN: the particle phases */
+#define OPX_PHASE_DIA 2   /* reductions / diagnostics */
+#define OPX_PHASE_LINKS 3 /* stepLinks */
+#define OPX_NUM_PHASES 4
+
+typedef struct opx_ctx opx_ctx;
+
+/* Settings subset that the field solver reads (physics/Settings.java:43-104,
+ * physics/grid/Grid.java:443-473). */
+typedef struct {
+    int ncolors;       /* 2 or 3 (Settings.numberOfColors) */
+    int dims[3];       /* grid cells per direction (Settings.gridCells) */
+    double a[3];       /* lattice spacing per direction (Settings.gridStep[s]) */
+    double dt;         /* temporal spacing (Settings.timeStep) */
+    double g;          /* gauge coupling (Settings.couplingConstant) */
+    int precision;     /* OPX_F64 or OPX_F32 */
+    int reunit_every;  /* OPX_F32: re-unitarise links every k steps (0 = never) */
+    int device;        /* CUDA device ordinal */
+    int flags;         /* reserved, 0 */
+} opx_config;
+
+/* BulkQuantitiesInTime columns (diagnostics/methods/BulkQuantitiesInTime.java:83-121),
+ * computed as FieldMeasurements does (physics/measurements/FieldMeasurements.java:68-231),
+ * accumulated in FP64 with compensated sums. */
+typedef struct {
+    double e2[3];      /* EFieldSquared.getSum(dir) */
+    double b2[3];      /* BFieldSquared.getSum(dir): mean of U and Unext plaquettes */
+    double px, py, pz; /* pressures */
+    double gauss;      /* GaussLaw.getSum(): mean squared Gauss violation */
+    double rho2;       /* TotalChargeSquared.getSum(): sqrt(sum rho^2)/V */
+    double e2_total;   /* E^2 column */
+    double b2_total;   /* B^2 column */
+} opx_observables;
+
+/* CGC particle list (physics/particles/CGCParticle.java, YangMillsParticle.java:13-25)
+ * as host arrays: pos0, pos1, vel : [n][3]; Q0, Q1 : [n][na] (reference algebra
+ * layout); dir : [n]; update_charge : [n]. */
+typedef struct {
+    long n;
+    double *pos0, *pos1, *vel, *Q0, *Q1;
+    int32_t *dir;
+    uint8_t *update_charge;
+} opx_particles;
+
+/* ---- lifetime ---- */
+/* new Grid(settings) + FieldSolver selection (Grid.java:443-473,
+ * Settings.applySimulationTypeSetting :540-581).  Links start as identity,
+ * fields at zero, every cell active and evaluatable (Cell.java:49-74). */
+int opx_create(const opx_config *cfg, opx_ctx **out);
+void opx_destroy(opx_ctx *ctx);
+const char *opx_last_error(const opx_ctx *ctx);
+int opx_version(void);
+
+/* ---- host <-> device (the Grid getters/setters, Grid.java:126-261) ---- */
+int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int layout);
+int opx_download(opx_ctx *ctx, int field, double *host, size_t count, int layout);
+/* Cell.isActive / Cell.isEvaluatable masks; NULL resets to all-true
+ * (Grid.setActiveRegion / setEvaluationRegion, Grid.java:978-1004). */
+int opx_set_active(opx_ctx *ctx, const uint8_t *mask, size_t count);
+int opx_set_evaluatable(opx_ctx *ctx, const uint8_t *mask, size_t count);
+
+/* ---- leapfrog (physics/fields/FastTYMSolver.java) ---- */
+/* FieldSolver.stepLinks -> UpdateLinks: Unext = exp(-i dt E) U (FastTYMSolver.java:34-38,65-84) */
+int opx_step_links(opx_ctx *ctx);
+/* FieldSolver.step -> CombinedUpdate (FastTYMSolver.java:24-63) */
+int opx_update_grid(opx_ctx *ctx);
+/* Grid.storeFields -> Cell.reassignLinks (Grid.java:591-593, Cell.java:173-177) */
+int opx_store_fields(opx_ctx *ctx);
+/* Simulation.initialize (Simulation.java:318-352) */
+int opx_initialize(opx_ctx *ctx);
+/* nsteps x Simulation.step without diagnostics (Simulation.java:373-435) */
+int opx_step(opx_ctx *ctx, int nsteps);
+/* Re-unitarise U and Unext (FP32 form; no counterpart in the reference). */
+int opx_reunitarize(opx_ctx *ctx);
+int opx_synchronize(opx_ctx *ctx);
+long opx_steps_done(const opx_ctx *ctx);
+
+/* ---- reductions / diagnostics ---- */
+int opx_reduce(opx_ctx *ctx, opx_observables *out);
+/* EnergyDensity.ComponentComputation (diagnostics/methods/EnergyDensity.java:119-166): V doubles */
+int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count);
+/* ProjectedEnergyDensity.EnergyDensityComputation (ProjectedEnergyDensity.java:114-179):
+ * 4 rows of dims[dir] doubles: T_el, T_mag, L_el, L_mag */
+int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count);
+/* Grid.getGaussConstraint at every cell (Grid.java:944-968), generator components [V][ngen] */
+int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count);
+
+/* ---- CPIC (physics/grid/CGCParticleInterpolationNGP.java,
+ *             physics/movement/solver/CGCParticleSolver.java) ---- */
+int opx_particles_upload(opx_ctx *ctx, const opx_particles *p);
+int opx_particles_download(opx_ctx *ctx, opx_particles *p);
+/* Particle phases of one Simulation.step (reassign != 0) or of
+ * Simulation.initialize (reassign == 0): charge density, positions, transport,
+ * charges, currents (Simulation.java:398-421, 329-347). */
+int opx_cpic_phases(opx_ctx *ctx, int reassign);
+
+/* ---- seeded synthetic initial conditions (no counterpart in the reference) ---- */
+/* U_i(x) = exp(i A_i^a(x) t_a), A ~ N(0, sigma_a^2); E_i^a(x) ~ N(0, sigma_e^2);
+ * same counter-based generator as the oracle. */
+int opx_init_random(opx_ctx *ctx, uint64_t seed, double sigma_a, double sigma_e);
+/* Project E onto Gauss's law by conjugate gradients (FP64 on the device):
+ * div(divT mu) = rho - div E, E <- E + divT mu. */
+int opx_gauss_project(opx_ctx *ctx, double tol_g2, int maxit, int *iters, double *final_g2);
+
+/* ---- timing (Simulation PerformanceTimer laps as CUDA events on the handle's stream) ---- */
+int opx_set_profiling(opx_ctx *ctx, int on);
+/* per phase: accumulated milliseconds and launch counts since profiling was enabled */
+int opx_phase_times(opx_ctx *ctx, double *ms, long *counts, int nphases);
+/* Time nsteps x opx_step with CUDA events recorded on the handle's stream. */
+int opx_time_steps(opx_ctx *ctx, int nsteps, double *ms);
+/* Number of kernels this handle has launched since creation. */
+long opx_kernel_launches(const opx_ctx *ctx);
+
+/* Page-locked host memory for transfers (cudaMallocHost / cudaFreeHost). */
+void *opx_host_alloc(size_t bytes);
+void opx_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

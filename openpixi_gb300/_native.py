@@ -1,0 +1,322 @@
+"""ctypes binding of libopixi_gpu.so (the C ABI declared in include/opixi.h).
+
+The library is built in-tree by ``openpixi_gb300.build`` (``__graft_entry__.build()``
+does it).  Loading fails loudly when it is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libopixi_gpu.so")
+
+OPX_OK = 0
+OPX_ERR_INVALID = -1
+OPX_ERR_CUDA = -2
+OPX_ERR_NOMEM = -3
+OPX_ERR_NUMERIC = -4
+OPX_ERR_UNSUPPORTED = -5
+OPX_ERR_TIMEOUT = -6
+
+OPX_F64 = 0
+OPX_F32 = 1
+
+FIELD_U, FIELD_UNEXT, FIELD_E, FIELD_J, FIELD_RHO = range(5)
+LAYOUT_REF, LAYOUT_GEN = 0, 1
+PHASE_EOM, PHASE_CPIC, PHASE_DIA, PHASE_LINKS = range(4)
+NUM_PHASES = 4
+
+# Every symbol include/opixi.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "opx_create", "opx_destroy", "opx_last_error", "opx_version",
+    "opx_upload", "opx_download", "opx_set_active", "opx_set_evaluatable",
+    "opx_step_links", "opx_update_grid", "opx_store_fields", "opx_initialize", "opx_step",
+    "opx_reunitarize", "opx_synchronize", "opx_steps_done",
+    "opx_reduce", "opx_energy_density", "opx_projected_energy", "opx_gauss_field",
+    "opx_particles_upload", "opx_particles_download", "opx_cpic_phases",
+    "opx_init_random", "opx_gauss_project",
+    "opx_set_profiling", "opx_phase_times", "opx_time_steps", "opx_kernel_launches",
+    "opx_host_alloc", "opx_host_free",
+]
+
+
+class OpixiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"opixi error {code}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("ncolors", C.c_int), ("dims", C.c_int * 3), ("a", C.c_double * 3),
+                ("dt", C.c_double), ("g", C.c_double), ("precision", C.c_int),
+                ("reunit_every", C.c_int), ("device", C.c_int), ("flags", C.c_int)]
+
+
+class Observables(C.Structure):
+    _fields_ = [("e2", C.c_double * 3), ("b2", C.c_double * 3), ("px", C.c_double),
+                ("py", C.c_double), ("pz", C.c_double), ("gauss", C.c_double),
+                ("rho2", C.c_double), ("e2_total", C.c_double), ("b2_total", C.c_double)]
+
+    def as_dict(self):
+        return {"e2": list(self.e2), "b2": list(self.b2), "px": self.px, "py": self.py, "pz": self.pz,
+                "gauss": self.gauss, "rho2": self.rho2, "e2_total": self.e2_total,
+                "b2_total": self.b2_total}
+
+
+class Particles(C.Structure):
+    _fields_ = [("n", C.c_long), ("pos0", C.c_void_p), ("pos1", C.c_void_p), ("vel", C.c_void_p),
+                ("Q0", C.c_void_p), ("Q1", C.c_void_p), ("dir", C.c_void_p),
+                ("update_charge", C.c_void_p)]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"libopixi_gpu.so not built ({p}); run openpixi_gb300.build.build()")
+    L = C.CDLL(p)
+    vp, sz, dp = C.c_void_p, C.c_size_t, C.POINTER(C.c_double)
+    sig = {
+        "opx_create": (C.c_int, [C.POINTER(Config), C.POINTER(vp)]),
+        "opx_destroy": (None, [vp]),
+        "opx_last_error": (C.c_char_p, [vp]),
+        "opx_version": (C.c_int, []),
+        "opx_upload": (C.c_int, [vp, C.c_int, vp, sz, C.c_int]),
+        "opx_download": (C.c_int, [vp, C.c_int, vp, sz, C.c_int]),
+        "opx_set_active": (C.c_int, [vp, vp, sz]),
+        "opx_set_evaluatable": (C.c_int, [vp, vp, sz]),
+        "opx_step_links": (C.c_int, [vp]),
+        "opx_update_grid": (C.c_int, [vp]),
+        "opx_store_fields": (C.c_int, [vp]),
+        "opx_initialize": (C.c_int, [vp]),
+        "opx_step": (C.c_int, [vp, C.c_int]),
+        "opx_reunitarize": (C.c_int, [vp]),
+        "opx_synchronize": (C.c_int, [vp]),
+        "opx_steps_done": (C.c_long, [vp]),
+        "opx_reduce": (C.c_int, [vp, C.POINTER(Observables)]),
+        "opx_energy_density": (C.c_int, [vp, vp, sz]),
+        "opx_projected_energy": (C.c_int, [vp, C.c_int, vp, sz]),
+        "opx_gauss_field": (C.c_int, [vp, vp, sz]),
+        "opx_particles_upload": (C.c_int, [vp, C.POINTER(Particles)]),
+        "opx_particles_download": (C.c_int, [vp, C.POINTER(Particles)]),
+        "opx_cpic_phases": (C.c_int, [vp, C.c_int]),
+        "opx_init_random": (C.c_int, [vp, C.c_uint64, C.c_double, C.c_double]),
+        "opx_gauss_project": (C.c_int, [vp, C.c_double, C.c_int, C.POINTER(C.c_int), dp]),
+        "opx_set_profiling": (C.c_int, [vp, C.c_int]),
+        "opx_phase_times": (C.c_int, [vp, dp, C.POINTER(C.c_long), C.c_int]),
+        "opx_time_steps": (C.c_int, [vp, C.c_int, dp]),
+        "opx_kernel_launches": (C.c_long, [vp]),
+        "opx_host_alloc": (vp, [sz]),
+        "opx_host_free": (None, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def ptr(a):
+    if a is None:
+        return None
+    assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"], "C-contiguous numpy array required"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Handle:
+    """Owning wrapper around one ``opx_ctx`` (one lattice on one GPU)."""
+
+    def __init__(self, ncolors, dims, a=(1.0, 1.0, 1.0), dt=0.05, g=1.0, precision=OPX_F64,
+                 reunit_every=0, device=0):
+        self.L = load()
+        if np.ndim(a) == 0:
+            a = (float(a),) * 3
+        cfg = Config(int(ncolors), (C.c_int * 3)(*[int(d) for d in dims]), (C.c_double * 3)(*a),
+                     float(dt), float(g), int(precision), int(reunit_every), int(device), 0)
+        h = C.c_void_p()
+        rc = self.L.opx_create(C.byref(cfg), C.byref(h))
+        if rc != OPX_OK:
+            raise OpixiError(rc, self.L.opx_last_error(None).decode())
+        self.h = h
+        self.ncolors = int(ncolors)
+        self.dims = tuple(int(d) for d in dims)
+        self.V = int(np.prod(self.dims))
+        self.precision = precision
+        self.ng = 18 if ncolors == 3 else 4
+        self.na_ref = 9 if ncolors == 3 else 3
+        self.ngen = 8 if ncolors == 3 else 3
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.opx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc != OPX_OK:
+            raise OpixiError(rc, self.L.opx_last_error(self.h).decode())
+        return rc
+
+    # ---- transfers ----
+    def _shape(self, field, layout):
+        na = self.na_ref if layout == LAYOUT_REF else self.ngen
+        if field in (FIELD_U, FIELD_UNEXT):
+            return (self.V, 3, self.ng)
+        if field in (FIELD_E, FIELD_J):
+            return (self.V, 3, na)
+        return (self.V, na)
+
+    def upload(self, field, arr, layout=LAYOUT_REF):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self.check(self.L.opx_upload(self.h, field, ptr(a), a.size, layout))
+
+    def download(self, field, layout=LAYOUT_REF, out=None):
+        shp = self._shape(field, layout)
+        out = np.empty(shp) if out is None else out
+        self.check(self.L.opx_download(self.h, field, ptr(out), out.size, layout))
+        return out
+
+    def set_active(self, mask):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        self.check(self.L.opx_set_active(self.h, ptr(m), 0 if m is None else m.size))
+
+    def set_evaluatable(self, mask):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        self.check(self.L.opx_set_evaluatable(self.h, ptr(m), 0 if m is None else m.size))
+
+    # ---- solver ----
+    def step_links(self):
+        self.check(self.L.opx_step_links(self.h))
+
+    def update_grid(self):
+        self.check(self.L.opx_update_grid(self.h))
+
+    def store_fields(self):
+        self.check(self.L.opx_store_fields(self.h))
+
+    def initialize(self):
+        self.check(self.L.opx_initialize(self.h))
+
+    def step(self, n=1):
+        self.check(self.L.opx_step(self.h, int(n)))
+
+    def reunitarize(self):
+        self.check(self.L.opx_reunitarize(self.h))
+
+    def synchronize(self):
+        self.check(self.L.opx_synchronize(self.h))
+
+    @property
+    def steps_done(self):
+        return self.L.opx_steps_done(self.h)
+
+    # ---- reductions ----
+    def reduce(self):
+        o = Observables()
+        self.check(self.L.opx_reduce(self.h, C.byref(o)))
+        return o
+
+    def energy_density(self):
+        out = np.empty(self.V)
+        self.check(self.L.opx_energy_density(self.h, ptr(out), out.size))
+        return out
+
+    def projected_energy(self, d):
+        out = np.empty(4 * self.dims[d])
+        self.check(self.L.opx_projected_energy(self.h, int(d), ptr(out), out.size))
+        return out.reshape(4, self.dims[d])
+
+    def gauss_field(self):
+        out = np.empty((self.V, self.ngen))
+        self.check(self.L.opx_gauss_field(self.h, ptr(out), out.size))
+        return out
+
+    # ---- particles ----
+    def particles_upload(self, pos0, pos1, vel, Q0, Q1, direction):
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (pos0, pos1, vel, Q0, Q1)]
+        d = np.ascontiguousarray(direction, dtype=np.int32)
+        self._pkeep = arrs + [d]
+        p = Particles(len(d), *[ptr(x) for x in arrs], ptr(d), None)
+        self.check(self.L.opx_particles_upload(self.h, C.byref(p)))
+        self.np = len(d)
+
+    def particles_download(self):
+        n = self.np
+        out = {k: np.empty((n, 3)) for k in ("pos0", "pos1", "vel")}
+        out["Q0"] = np.empty((n, self.na_ref))
+        out["Q1"] = np.empty((n, self.na_ref))
+        out["dir"] = np.empty(n, np.int32)
+        out["update_charge"] = np.empty(n, np.uint8)
+        p = Particles(n, ptr(out["pos0"]), ptr(out["pos1"]), ptr(out["vel"]), ptr(out["Q0"]),
+                      ptr(out["Q1"]), ptr(out["dir"]), ptr(out["update_charge"]))
+        self.check(self.L.opx_particles_download(self.h, C.byref(p)))
+        return out
+
+    def cpic_phases(self, reassign=True):
+        self.check(self.L.opx_cpic_phases(self.h, 1 if reassign else 0))
+
+    # ---- initial conditions ----
+    def init_random(self, seed, sigma_a, sigma_e):
+        self.check(self.L.opx_init_random(self.h, C.c_uint64(seed), float(sigma_a), float(sigma_e)))
+
+    def gauss_project(self, tol=1e-26, maxit=5000):
+        it = C.c_int()
+        g2 = C.c_double()
+        self.check(self.L.opx_gauss_project(self.h, float(tol), int(maxit), C.byref(it), C.byref(g2)))
+        return it.value, g2.value
+
+    # ---- timing ----
+    def set_profiling(self, on=True):
+        self.check(self.L.opx_set_profiling(self.h, 1 if on else 0))
+
+    def phase_times(self):
+        ms = (C.c_double * NUM_PHASES)()
+        n = (C.c_long * NUM_PHASES)()
+        self.check(self.L.opx_phase_times(self.h, ms, n, NUM_PHASES))
+        return list(ms), list(n)
+
+    def time_steps(self, n):
+        ms = C.c_double()
+        self.check(self.L.opx_time_steps(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    @property
+    def kernel_launches(self):
+        return self.L.opx_kernel_launches(self.h)
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory from opx_host_alloc."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.L = load()
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.p = self.L.opx_host_alloc(n)
+        if not self.p:
+            raise MemoryError("opx_host_alloc failed")
+        buf = (C.c_char * n).from_address(self.p)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.p:
+            self.array = None
+            self.L.opx_host_free(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

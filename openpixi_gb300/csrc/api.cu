@@ -1,0 +1,568 @@
+// api.cu -- the C ABI of libopixi_gpu.so (declared in include/opixi.h).
+//
+// A handle is one lattice on one GPU with its own CUDA stream: the device
+// counterpart of physics/grid/Grid.java plus the FastTYMSolver selected by
+// physics/Settings.java:540-581, the CGC particle list and the diagnostics.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace opx;
+
+struct opx_ctx {
+    Ctx c;
+};
+
+static std::string g_create_error;
+
+#define API_CHECK(ctx)                                   \
+    do {                                                 \
+        if (!(ctx)) return OPX_ERR_INVALID;              \
+    } while (0)
+
+static int cuda_fail(Ctx &c, const char *where, cudaError_t e) {
+    c.err = std::string(where) + ": " + cudaGetErrorString(e);
+    return OPX_ERR_CUDA;
+}
+
+// Check for launch errors of the work queued so far (cheap, no sync).
+static int check_launch(Ctx &c, const char *where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, where, e);
+    return OPX_OK;
+}
+
+static int sync_check(Ctx &c, const char *where) {
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, where, e);
+    return check_launch(c, where);
+}
+
+template <typename R>
+__global__ void k_fill_identity(R *U, long V, int ng, int nc) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over 3*ng*V
+    if (t >= 3L * ng * V) return;
+    const long plane = t / V;
+    const int c = (int)(plane % ng);
+    const bool one = nc == 3 ? (c == 0 || c == 4 || c == 8) : (c == 0);
+    U[t] = one ? R(1) : R(0);
+}
+
+static void fill_identity(Ctx &c, void *U) {
+    const long n = 3L * c.ng * c.L.V;
+    if (c.prec == OPX_F64) k_fill_identity<double><<<grid_for(n, 256), 256, 0, c.stream>>>((double *)U, c.L.V, c.ng, c.nc);
+    else k_fill_identity<float><<<grid_for(n, 256), 256, 0, c.stream>>>((float *)U, c.L.V, c.ng, c.nc);
+    c.launches++;
+}
+
+static void release(Ctx &c) {
+    cpic_free(c);
+    void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.status};
+    for (void *p : dev) if (p) cudaFree(p);
+    if (c.red_host) cudaFreeHost(c.red_host);
+    if (c.status_host) cudaFreeHost(c.status_host);
+    if (c.ev0) cudaEventDestroy(c.ev0);
+    if (c.ev1) cudaEventDestroy(c.ev1);
+    if (c.stream) cudaStreamDestroy(c.stream);
+}
+
+extern "C" {
+
+int opx_version(void) { return 10000; }
+
+const char *opx_last_error(const opx_ctx *ctx) {
+    if (!ctx) return g_create_error.c_str();
+    return ctx->c.err.c_str();
+}
+
+int opx_create(const opx_config *cfg, opx_ctx **out) {
+    if (!cfg || !out) { g_create_error = "opx_create: null argument"; return OPX_ERR_INVALID; }
+    *out = nullptr;
+    if (cfg->ncolors != 2 && cfg->ncolors != 3) { g_create_error = "opx_create: ncolors must be 2 or 3"; return OPX_ERR_INVALID; }
+    if (cfg->precision != OPX_F64 && cfg->precision != OPX_F32) { g_create_error = "opx_create: precision must be OPX_F64 or OPX_F32"; return OPX_ERR_INVALID; }
+    long V = 1;
+    for (int i = 0; i < 3; i++) {
+        if (cfg->dims[i] < 1) { g_create_error = "opx_create: dims must be >= 1"; return OPX_ERR_INVALID; }
+        if (!(cfg->a[i] > 0)) { g_create_error = "opx_create: lattice spacings must be > 0"; return OPX_ERR_INVALID; }
+        V *= cfg->dims[i];
+    }
+    if (V * 4 > 2147483647L) { g_create_error = "opx_create: lattice too large (4*V must fit in int32)"; return OPX_ERR_INVALID; }
+    if (!(cfg->dt > 0) || !(cfg->g > 0)) { g_create_error = "opx_create: dt and g must be > 0"; return OPX_ERR_INVALID; }
+    if (cfg->reunit_every < 0) { g_create_error = "opx_create: reunit_every must be >= 0"; return OPX_ERR_INVALID; }
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) { g_create_error = std::string("opx_create: ") + cudaGetErrorString(e); return OPX_ERR_CUDA; }
+    opx_ctx *h = new (std::nothrow) opx_ctx();
+    if (!h) { g_create_error = "opx_create: host allocation failed"; return OPX_ERR_NOMEM; }
+    Ctx &c = h->c;
+    c.cfg = *cfg;
+    c.L = make_lat(cfg->dims, cfg->a, cfg->dt, cfg->g);
+    c.nc = cfg->ncolors;
+    c.ng = c.nc == 3 ? 18 : 4;
+    c.na = c.nc == 3 ? 8 : 3;
+    c.na_ref = c.nc == 3 ? 9 : 3;
+    c.prec = cfg->precision;
+    c.rsize = c.prec == OPX_F64 ? 8 : 4;
+    bool ok = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) == cudaSuccess;
+    auto al = [&](void **p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) { ok = false; *p = nullptr; } };
+    const size_t nU = (size_t)V * 3 * c.ng, nE = (size_t)V * 3 * c.na;
+    al(&c.U, nU * c.rsize);
+    al(&c.Unext, nU * c.rsize);
+    al(&c.E, nE * c.rsize);
+    // J and rho are FP64 when particles can be attached (FP64 handles), storage precision otherwise
+    al(&c.J, nE * c.rsize);
+    al(&c.rho, (size_t)V * c.na * c.rsize);
+    c.red_blocks = (int)std::min<long>(grid_for(V, 256), 4L * 152);
+    al((void **)&c.red_part, sizeof(double) * 2 * 8 * c.red_blocks);
+    al((void **)&c.red_out, sizeof(double) * 16);
+    al((void **)&c.status, sizeof(unsigned));
+    if (ok && cudaMallocHost((void **)&c.red_host, sizeof(double) * 16) != cudaSuccess) ok = false;
+    if (ok && cudaMallocHost((void **)&c.status_host, sizeof(unsigned)) != cudaSuccess) ok = false;
+    if (ok && (cudaEventCreate(&c.ev0) != cudaSuccess || cudaEventCreate(&c.ev1) != cudaSuccess)) ok = false;
+    if (!ok) {
+        release(c);
+        delete h;
+        g_create_error = "opx_create: out of device memory";
+        cudaGetLastError();
+        return OPX_ERR_NOMEM;
+    }
+    fill_identity(c, c.U);
+    fill_identity(c, c.Unext);
+    cudaMemsetAsync(c.E, 0, nE * c.rsize, c.stream);
+    cudaMemsetAsync(c.J, 0, nE * c.rsize, c.stream);
+    cudaMemsetAsync(c.rho, 0, (size_t)V * c.na * c.rsize, c.stream);
+    cudaMemsetAsync(c.status, 0, sizeof(unsigned), c.stream);
+    if (sync_check(c, "opx_create") != OPX_OK) {
+        g_create_error = c.err;
+        release(c);
+        delete h;
+        return OPX_ERR_CUDA;
+    }
+    *out = h;
+    return OPX_OK;
+}
+
+void opx_destroy(opx_ctx *ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->c.stream);
+    release(ctx->c);
+    delete ctx;
+}
+
+static int ensure_staging(Ctx &c, size_t ndoubles) {
+    if (c.staging_len >= ndoubles) return OPX_OK;
+    if (c.staging) cudaFree(c.staging);
+    c.staging = nullptr;
+    c.staging_len = 0;
+    if (cudaMalloc(&c.staging, ndoubles * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        c.err = "staging buffer: out of device memory";
+        return OPX_ERR_NOMEM;
+    }
+    c.staging_len = ndoubles;
+    return OPX_OK;
+}
+
+static int field_count(const Ctx &c, int field, int layout, size_t *n, int *ndir) {
+    const int na_host = (layout == OPX_LAYOUT_REF) ? c.na_ref : c.na;
+    switch (field) {
+    case OPX_FIELD_U:
+    case OPX_FIELD_UNEXT: *n = (size_t)c.L.V * 3 * c.ng; *ndir = 3; return OPX_OK;
+    case OPX_FIELD_E:
+    case OPX_FIELD_J: *n = (size_t)c.L.V * 3 * na_host; *ndir = 3; return OPX_OK;
+    case OPX_FIELD_RHO: *n = (size_t)c.L.V * na_host; *ndir = 1; return OPX_OK;
+    }
+    return OPX_ERR_INVALID;
+}
+
+int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int layout) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    size_t n;
+    int ndir;
+    if (!host || (layout != OPX_LAYOUT_REF && layout != OPX_LAYOUT_GEN) || field_count(c, field, layout, &n, &ndir)) {
+        c.err = "opx_upload: invalid field, layout or null buffer";
+        return OPX_ERR_INVALID;
+    }
+    if (count != n) {
+        c.err = "opx_upload: count " + std::to_string(count) + " != expected " + std::to_string(n);
+        return OPX_ERR_INVALID;
+    }
+    int rc = ensure_staging(c, n);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(c.staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, "opx_upload", e);
+    switch (field) {
+    case OPX_FIELD_U: launch_links_from_ref(c, c.staging, c.U); break;
+    case OPX_FIELD_UNEXT: launch_links_from_ref(c, c.staging, c.Unext); break;
+    case OPX_FIELD_E: launch_alg_from_host(c, c.staging, c.E, 3, layout); break;
+    case OPX_FIELD_J: launch_alg_from_host(c, c.staging, c.J, 3, layout); c.j_nonzero = true; break;
+    case OPX_FIELD_RHO: launch_alg_from_host(c, c.staging, c.rho, 1, layout); break;
+    }
+    return sync_check(c, "opx_upload");
+}
+
+int opx_download(opx_ctx *ctx, int field, double *host, size_t count, int layout) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    size_t n;
+    int ndir;
+    if (!host || (layout != OPX_LAYOUT_REF && layout != OPX_LAYOUT_GEN) || field_count(c, field, layout, &n, &ndir)) {
+        c.err = "opx_download: invalid field, layout or null buffer";
+        return OPX_ERR_INVALID;
+    }
+    if (count != n) {
+        c.err = "opx_download: count " + std::to_string(count) + " != expected " + std::to_string(n);
+        return OPX_ERR_INVALID;
+    }
+    int rc = ensure_staging(c, n);
+    if (rc) return rc;
+    switch (field) {
+    case OPX_FIELD_U: launch_links_to_ref(c, c.U, c.staging); break;
+    case OPX_FIELD_UNEXT: launch_links_to_ref(c, c.Unext, c.staging); break;
+    case OPX_FIELD_E: launch_alg_to_host(c, c.E, c.staging, 3, layout); break;
+    case OPX_FIELD_J: launch_alg_to_host(c, c.J, c.staging, 3, layout); break;
+    case OPX_FIELD_RHO: launch_alg_to_host(c, c.rho, c.staging, 1, layout); break;
+    }
+    cudaError_t e = cudaMemcpyAsync(host, c.staging, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, "opx_download", e);
+    return sync_check(c, "opx_download");
+}
+
+static int set_mask(Ctx &c, uint8_t **dst, const uint8_t *mask, size_t count, const char *where) {
+    if (!mask) {
+        if (*dst) { cudaStreamSynchronize(c.stream); cudaFree(*dst); }
+        *dst = nullptr;
+        return OPX_OK;
+    }
+    if (count != (size_t)c.L.V) { c.err = std::string(where) + ": count must equal the number of cells"; return OPX_ERR_INVALID; }
+    if (!*dst && cudaMalloc((void **)dst, c.L.V) != cudaSuccess) { cudaGetLastError(); c.err = std::string(where) + ": out of device memory"; return OPX_ERR_NOMEM; }
+    cudaError_t e = cudaMemcpyAsync(*dst, mask, c.L.V, cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, where, e);
+    return sync_check(c, where);
+}
+
+int opx_set_active(opx_ctx *ctx, const uint8_t *mask, size_t count) {
+    API_CHECK(ctx);
+    return set_mask(ctx->c, &ctx->c.active, mask, count, "opx_set_active");
+}
+
+int opx_set_evaluatable(opx_ctx *ctx, const uint8_t *mask, size_t count) {
+    API_CHECK(ctx);
+    return set_mask(ctx->c, &ctx->c.eval, mask, count, "opx_set_evaluatable");
+}
+
+static void phase_begin(Ctx &c) {
+    if (c.profiling) cudaEventRecord(c.ev0, c.stream);
+}
+static void phase_end(Ctx &c, int phase) {
+    if (!c.profiling) return;
+    cudaEventRecord(c.ev1, c.stream);
+    cudaEventSynchronize(c.ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    c.phase_ms[phase] += ms;
+    c.phase_n[phase] += 1;
+}
+
+int opx_step_links(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    phase_begin(c);
+    launch_update_links(c);
+    phase_end(c, OPX_PHASE_LINKS);
+    return check_launch(c, "opx_step_links");
+}
+
+int opx_update_grid(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    phase_begin(c);
+    launch_update_grid(c, false);
+    phase_end(c, OPX_PHASE_EOM);
+    return check_launch(c, "opx_update_grid");
+}
+
+int opx_store_fields(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    std::swap(ctx->c.U, ctx->c.Unext);
+    return OPX_OK;
+}
+
+int opx_reunitarize(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    launch_reunit(c, c.U);
+    launch_reunit(c, c.Unext);
+    return check_launch(c, "opx_reunitarize");
+}
+
+static int cpic_ok(Ctx &c, const char *where) {
+    if (c.prec != OPX_F64) {
+        c.err = std::string(where) + ": particles require an OPX_F64 handle";
+        return OPX_ERR_UNSUPPORTED;
+    }
+    return OPX_OK;
+}
+
+int opx_cpic_phases(opx_ctx *ctx, int reassign) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    int rc = cpic_ok(c, "opx_cpic_phases");
+    if (rc) return rc;
+    phase_begin(c);
+    launch_cpic_phases(c, reassign);
+    phase_end(c, OPX_PHASE_CPIC);
+    return check_launch(c, "opx_cpic_phases");
+}
+
+int opx_initialize(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    int rc = opx_step_links(ctx);
+    if (rc) return rc;
+    if (c.P.n > 0) return opx_cpic_phases(ctx, 0);
+    return OPX_OK;
+}
+
+static int one_step(Ctx &c) {
+    c.steps++;
+    std::swap(c.U, c.Unext);  // storeFields
+    const bool reunit = c.prec == OPX_F32 && c.cfg.reunit_every > 0 && (c.steps % c.cfg.reunit_every) == 0;
+    phase_begin(c);
+    launch_update_grid(c, reunit);
+    phase_end(c, OPX_PHASE_EOM);
+    if (c.P.n > 0) {
+        phase_begin(c);
+        launch_cpic_phases(c, 1);
+        phase_end(c, OPX_PHASE_CPIC);
+    }
+    return OPX_OK;
+}
+
+int opx_step(opx_ctx *ctx, int nsteps) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (nsteps < 0) { c.err = "opx_step: nsteps < 0"; return OPX_ERR_INVALID; }
+    for (int k = 0; k < nsteps; k++) one_step(c);
+    return check_launch(c, "opx_step");
+}
+
+int opx_synchronize(opx_ctx *ctx) {
+    API_CHECK(ctx);
+    return sync_check(ctx->c, "opx_synchronize");
+}
+
+long opx_steps_done(const opx_ctx *ctx) { return ctx ? ctx->c.steps : -1; }
+
+int opx_reduce(opx_ctx *ctx, opx_observables *out) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (!out) { c.err = "opx_reduce: null output"; return OPX_ERR_INVALID; }
+    phase_begin(c);
+    launch_bulk(c);
+    cudaMemcpyAsync(c.red_host, c.red_out, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream);
+    int rc = sync_check(c, "opx_reduce");
+    phase_end(c, OPX_PHASE_DIA);
+    if (rc) return rc;
+    const double V = (double)c.L.V;
+    const double *r = c.red_host;
+    double es[3], bs[3];
+    for (int i = 0; i < 3; i++) { es[i] = r[i] / V; bs[i] = r[3 + i] / V; out->e2[i] = es[i]; out->b2[i] = bs[i]; }
+    out->px = -es[0] + es[1] + es[2] - bs[0] + bs[1] + bs[2];
+    out->py = +es[0] - es[1] + es[2] + bs[0] - bs[1] + bs[2];
+    out->pz = +es[0] + es[1] - es[2] + bs[0] + bs[1] - bs[2];
+    out->gauss = r[6] / V;
+    out->rho2 = std::sqrt(r[7]) / V;
+    out->e2_total = es[0] + es[1] + es[2];
+    out->b2_total = bs[0] + bs[1] + bs[2];
+    for (int q = 0; q < 8; q++)
+        if (!std::isfinite(r[q])) {
+            c.err = "opx_reduce: non-finite field values (NaN/Inf) on the lattice";
+            return OPX_ERR_NUMERIC;
+        }
+    return OPX_OK;
+}
+
+int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (!host_out || count != (size_t)c.L.V) { c.err = "opx_energy_density: output must hold V doubles"; return OPX_ERR_INVALID; }
+    int rc = ensure_staging(c, c.L.V);
+    if (rc) return rc;
+    launch_energy_density(c, c.staging);
+    cudaMemcpyAsync(host_out, c.staging, sizeof(double) * c.L.V, cudaMemcpyDeviceToHost, c.stream);
+    return sync_check(c, "opx_energy_density");
+}
+
+int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (dir < 0 || dir > 2) { c.err = "opx_projected_energy: dir must be 0, 1 or 2"; return OPX_ERR_INVALID; }
+    const size_t n = 4 * (size_t)c.L.n[dir];
+    if (!host_out || count != n) { c.err = "opx_projected_energy: output must hold 4*dims[dir] doubles"; return OPX_ERR_INVALID; }
+    int rc = ensure_staging(c, n);
+    if (rc) return rc;
+    launch_projected_energy(c, dir, c.staging);
+    cudaMemcpyAsync(host_out, c.staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
+    return sync_check(c, "opx_projected_energy");
+}
+
+int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    const size_t n = (size_t)c.L.V * c.na;
+    if (!host_out || count != n) { c.err = "opx_gauss_field: output must hold V*ngen doubles"; return OPX_ERR_INVALID; }
+    int rc = ensure_staging(c, n);
+    if (rc) return rc;
+    launch_gauss_field(c, c.staging);
+    cudaMemcpyAsync(host_out, c.staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
+    return sync_check(c, "opx_gauss_field");
+}
+
+int opx_particles_upload(opx_ctx *ctx, const opx_particles *p) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    int rc = cpic_ok(c, "opx_particles_upload");
+    if (rc) return rc;
+    if (!p || p->n < 0) { c.err = "opx_particles_upload: invalid particle list"; return OPX_ERR_INVALID; }
+    const long n = p->n;
+    if (n > 0 && (!p->pos0 || !p->pos1 || !p->vel || !p->Q0 || !p->Q1 || !p->dir)) {
+        c.err = "opx_particles_upload: null array";
+        return OPX_ERR_INVALID;
+    }
+    if (n >= 2147483647L / 2) { c.err = "opx_particles_upload: too many particles"; return OPX_ERR_INVALID; }
+    for (long k = 0; k < n; k++)
+        if (p->dir[k] < 0 || p->dir[k] > 2) { c.err = "opx_particles_upload: direction must be 0, 1 or 2"; return OPX_ERR_INVALID; }
+    rc = cpic_alloc(c, n);
+    if (rc) return rc;
+    if (n == 0) return OPX_OK;
+    const int nar = c.na_ref;
+    std::vector<double> t(3 * n);
+    auto put3 = [&](const double *src, double *dst) {
+        for (long k = 0; k < n; k++) for (int i = 0; i < 3; i++) t[i * n + k] = src[k * 3 + i];
+        return cudaMemcpy(dst, t.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice);
+    };
+    std::vector<double> tq((size_t)nar * n);
+    auto putq = [&](const double *src, double *dst) {
+        for (long k = 0; k < n; k++) for (int a = 0; a < nar; a++) tq[a * n + k] = src[k * nar + a];
+        return cudaMemcpy(dst, tq.data(), sizeof(double) * nar * n, cudaMemcpyHostToDevice);
+    };
+    std::vector<int8_t> d8(n);
+    for (long k = 0; k < n; k++) d8[k] = (int8_t)p->dir[k];
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = put3(p->pos0, c.P.pos0);
+    if (e == cudaSuccess) e = put3(p->pos1, c.P.pos1);
+    if (e == cudaSuccess) e = put3(p->vel, c.P.vel);
+    if (e == cudaSuccess) e = putq(p->Q0, c.P.q0);
+    if (e == cudaSuccess) e = putq(p->Q1, c.P.q1);
+    if (e == cudaSuccess) e = cudaMemcpy(c.P.dir, d8.data(), n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, "opx_particles_upload", e);
+    return OPX_OK;
+}
+
+int opx_particles_download(opx_ctx *ctx, opx_particles *p) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (!p || p->n != c.P.n) { c.err = "opx_particles_download: n must equal the uploaded count"; return OPX_ERR_INVALID; }
+    const long n = p->n;
+    if (n == 0) return OPX_OK;
+    int rc = sync_check(c, "opx_particles_download");
+    if (rc) return rc;
+    const int nar = c.na_ref;
+    std::vector<double> t(3 * n), tq((size_t)nar * n);
+    auto get3 = [&](const double *src, double *dst) {
+        cudaError_t e = cudaMemcpy(t.data(), src, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost);
+        for (long k = 0; k < n; k++) for (int i = 0; i < 3; i++) dst[k * 3 + i] = t[i * n + k];
+        return e;
+    };
+    auto getq = [&](const double *src, double *dst) {
+        cudaError_t e = cudaMemcpy(tq.data(), src, sizeof(double) * nar * n, cudaMemcpyDeviceToHost);
+        for (long k = 0; k < n; k++) for (int a = 0; a < nar; a++) dst[k * nar + a] = tq[a * n + k];
+        return e;
+    };
+    cudaError_t e = cudaSuccess;
+    if (p->pos0 && e == cudaSuccess) e = get3(c.P.pos0, p->pos0);
+    if (p->pos1 && e == cudaSuccess) e = get3(c.P.pos1, p->pos1);
+    if (p->vel && e == cudaSuccess) e = get3(c.P.vel, p->vel);
+    if (p->Q0 && e == cudaSuccess) e = getq(c.P.q0, p->Q0);
+    if (p->Q1 && e == cudaSuccess) e = getq(c.P.q1, p->Q1);
+    if (p->dir && e == cudaSuccess) {
+        std::vector<int8_t> d8(n);
+        e = cudaMemcpy(d8.data(), c.P.dir, n, cudaMemcpyDeviceToHost);
+        for (long k = 0; k < n; k++) p->dir[k] = d8[k];
+    }
+    if (p->update_charge) std::memset(p->update_charge, 0, n);
+    if (e != cudaSuccess) return cuda_fail(c, "opx_particles_download", e);
+    return OPX_OK;
+}
+
+int opx_init_random(opx_ctx *ctx, uint64_t seed, double sigma_a, double sigma_e) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (!(sigma_a >= 0) || !(sigma_e >= 0)) { c.err = "opx_init_random: sigmas must be >= 0"; return OPX_ERR_INVALID; }
+    int rc = ic_init_random(c, seed, sigma_a, sigma_e);
+    if (rc) return rc;
+    return sync_check(c, "opx_init_random");
+}
+
+int opx_gauss_project(opx_ctx *ctx, double tol_g2, int maxit, int *iters, double *final_g2) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (!(tol_g2 > 0) || maxit < 0) { c.err = "opx_gauss_project: tol must be > 0 and maxit >= 0"; return OPX_ERR_INVALID; }
+    return ic_gauss_project(c, tol_g2, maxit, iters, final_g2);
+}
+
+int opx_set_profiling(opx_ctx *ctx, int on) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    c.profiling = on != 0;
+    for (int k = 0; k < OPX_NUM_PHASES; k++) { c.phase_ms[k] = 0; c.phase_n[k] = 0; }
+    return OPX_OK;
+}
+
+int opx_phase_times(opx_ctx *ctx, double *ms, long *counts, int nphases) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    for (int k = 0; k < nphases && k < OPX_NUM_PHASES; k++) {
+        if (ms) ms[k] = c.phase_ms[k];
+        if (counts) counts[k] = c.phase_n[k];
+    }
+    return OPX_OK;
+}
+
+int opx_time_steps(opx_ctx *ctx, int nsteps, double *ms) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (nsteps < 0 || !ms) { c.err = "opx_time_steps: invalid arguments"; return OPX_ERR_INVALID; }
+    const bool prof = c.profiling;
+    c.profiling = false;
+    cudaEventRecord(c.ev0, c.stream);
+    for (int k = 0; k < nsteps; k++) one_step(c);
+    cudaEventRecord(c.ev1, c.stream);
+    cudaError_t e = cudaEventSynchronize(c.ev1);
+    c.profiling = prof;
+    if (e != cudaSuccess) return cuda_fail(c, "opx_time_steps", e);
+    float f = 0.f;
+    cudaEventElapsedTime(&f, c.ev0, c.ev1);
+    *ms = f;
+    return check_launch(c, "opx_time_steps");
+}
+
+long opx_kernel_launches(const opx_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
+
+void *opx_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return p;
+}
+
+void opx_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// internal.h -- handle state and kernel launchers shared by the translation units
+// of libopixi_gpu.so.  Not part of the public ABI (include/opixi.h is).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/opixi.h"
+#include "lattice.cuh"
+
+namespace opx {
+
+// Device status word bits (read back by the host after each API call that
+// checks numerics).
+enum : unsigned {
+    STATUS_NAN = 1u,        // a NaN/Inf was produced
+    STATUS_CG_DIVERGED = 2u,
+};
+
+struct Particles {
+    long n = 0, cap = 0;
+    double *pos0 = nullptr, *pos1 = nullptr, *vel = nullptr;  // [3][n] each
+    double *q0 = nullptr, *q1 = nullptr;                        // [na_ref][n]
+    int8_t *dir = nullptr;
+    // deposition scratch
+    int *key_rho = nullptr, *key_j = nullptr;                   // [n]
+    double *val_rho = nullptr, *val_j = nullptr;                // [na_ref][n]
+    int *count = nullptr, *offset = nullptr, *cursor = nullptr; // [4V] (+1)
+    int *slots = nullptr;                                       // [2n]
+    int *scan_tmp = nullptr;
+    long scan_tmp_len = 0;
+};
+
+struct Ctx {
+    opx_config cfg;
+    Lat L;
+    int nc = 2, ng = 4, na = 3, na_ref = 3;  // reals per link / generator comps / reference algebra reals
+    int prec = OPX_F64;
+    size_t rsize = 8;  // bytes per real on the device
+    cudaStream_t stream = nullptr;
+    void *U = nullptr, *Unext = nullptr, *E = nullptr, *J = nullptr, *rho = nullptr;
+    uint8_t *active = nullptr, *eval = nullptr;  // null = all true
+    bool j_nonzero = false;
+    double *staging = nullptr;
+    size_t staging_len = 0;  // doubles
+    double *red_part = nullptr;
+    int red_blocks = 0;
+    double *red_out = nullptr;     // device
+    double *red_host = nullptr;    // pinned
+    unsigned *status = nullptr;    // device status word
+    unsigned *status_host = nullptr;
+    long steps = 0;
+    long launches = 0;
+    Particles P;
+    bool profiling = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double phase_ms[OPX_NUM_PHASES] = {0, 0, 0, 0};
+    long phase_n[OPX_NUM_PHASES] = {0, 0, 0, 0};
+    std::string err;
+};
+
+// ---- launchers (field_kernels.cu) ----
+void launch_update_grid(Ctx &c, bool reunit);
+void launch_update_links(Ctx &c);
+void launch_reunit(Ctx &c, void *links);
+// ---- reductions (reduce_kernels.cu) ----
+void launch_bulk(Ctx &c);  // result in c.red_out[0..7]
+void launch_energy_density(Ctx &c, double *dev_out);
+void launch_projected_energy(Ctx &c, int dir, double *dev_out);
+void launch_gauss_field(Ctx &c, double *dev_out);
+// ---- conversions (convert_kernels.cu) ----
+void launch_links_from_ref(Ctx &c, const double *src, void *dst);
+void launch_links_to_ref(Ctx &c, const void *src, double *dst);
+void launch_alg_from_host(Ctx &c, const double *src, void *dst, int ndir, int layout);
+void launch_alg_to_host(Ctx &c, const void *src, double *dst, int ndir, int layout);
+// ---- initial conditions (ic_kernels.cu) ----
+int ic_init_random(Ctx &c, uint64_t seed, double sigma_a, double sigma_e);
+int ic_gauss_project(Ctx &c, double tol, int maxit, int *iters, double *final_g2);
+// ---- CPIC (cpic_kernels.cu) ----
+int cpic_alloc(Ctx &c, long n);
+void cpic_free(Ctx &c);
+void launch_cpic_phases(Ctx &c, int reassign);
+
+int grid_for(long n, int block);
+
+}  // namespace opx

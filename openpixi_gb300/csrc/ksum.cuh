@@ -1,0 +1,48 @@
+// ksum.cuh -- compensated FP64 accumulation (TwoSum / Neumaier) and the
+// deterministic block reduction used by every reduction kernel.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace opx {
+
+struct KSum {
+    double s, c;
+};
+__device__ __forceinline__ void two_sum_add(KSum &a, double x) {
+    double t = a.s + x;
+    double z = t - a.s;
+    a.c += (a.s - (t - z)) + (x - z);
+    a.s = t;
+}
+__device__ __forceinline__ void ksum_merge(KSum &a, const KSum &b) {
+    two_sum_add(a, b.s);
+    a.c += b.c;
+}
+
+// Reduce NQ compensated sums over a block (blockDim.x a multiple of 32, at most
+// 1024).  Thread q < NQ of the block receives the block total of quantity q.
+template <int NQ>
+__device__ __forceinline__ KSum block_reduce(KSum *acc, int &qout) {
+    __shared__ double sh_s[NQ][32], sh_c[NQ][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        KSum v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
+            ksum_merge(v, w);
+        }
+        if (lane == 0) { sh_s[q][warp] = v.s; sh_c[q][warp] = v.c; }
+    }
+    __syncthreads();
+    KSum v{0.0, 0.0};
+    qout = -1;
+    if (threadIdx.x < NQ) {
+        const int q = threadIdx.x;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) ksum_merge(v, KSum{sh_s[q][w], sh_c[q][w]});
+        qout = q;
+    }
+    return v;
+}
+
+}  // namespace opx

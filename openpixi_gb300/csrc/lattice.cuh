@@ -1,0 +1,124 @@
+// lattice.cuh -- lattice geometry and the structure-of-arrays field layout.
+//
+// Site index s = ((x0*N1)+x1)*N2+x2, dimension 0 slowest (Grid.java:757-770),
+// so dimension 2 is contiguous and a warp reads 32 consecutive sites.
+// Fields are stored as planes: component c of direction d of every site is a
+// contiguous array of V values,
+//   links  U[d][c][s]  (c < NG: 4 for SU(2), 18 for SU(3))
+//   fields E[d][a][s]  (a < NA: 3 for SU(2), 8 for SU(3), generator components)
+//   rho    [a][s]
+// which makes every per-component access of a thread block fully coalesced.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "group.cuh"
+
+namespace opx {
+
+struct Lat {
+    int n[3];
+    long V;
+    long stride[3];  // n1*n2, n2, 1
+    double a[3];
+    double dt, g;
+};
+
+__host__ inline Lat make_lat(const int *dims, const double *a, double dt, double g) {
+    Lat L;
+    for (int i = 0; i < 3; i++) { L.n[i] = dims[i]; L.a[i] = a[i]; }
+    L.V = (long)dims[0] * dims[1] * dims[2];
+    L.stride[2] = 1;
+    L.stride[1] = dims[2];
+    L.stride[0] = (long)dims[1] * dims[2];
+    L.dt = dt;
+    L.g = g;
+    return L;
+}
+
+// Periodic neighbour offsets of site s (Grid.shift, Grid.java:802-823).
+struct Nbr {
+    long fwd[3];  // index of x + d
+    long bwd[3];  // index of x - d
+};
+
+__device__ __forceinline__ void site_coords(const Lat &L, long s, int *x) {
+    long t = s / L.n[2];
+    x[2] = (int)(s - t * L.n[2]);
+    long u = t / L.n[1];
+    x[1] = (int)(t - u * L.n[1]);
+    x[0] = (int)u;
+}
+
+__device__ __forceinline__ Nbr neighbours(const Lat &L, long s, const int *x) {
+    Nbr nb;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        long st = L.stride[d];
+        long wrap = (long)(L.n[d] - 1) * st;
+        nb.fwd[d] = x[d] == L.n[d] - 1 ? s - wrap : s + st;
+        nb.bwd[d] = x[d] == 0 ? s + wrap : s - st;
+    }
+    return nb;
+}
+
+// Structure-of-arrays views
+template <class G, typename R> struct LinkPlanes {
+    R *p;
+    long V;
+    __device__ __forceinline__ typename G::M load(int d, long s) const;
+    __device__ __forceinline__ void store(int d, long s, const typename G::M &m) const;
+};
+
+template <typename R> struct LinkPlanes<SU2<R>, R> {
+    R *p;
+    long V;
+    __device__ __forceinline__ Q2<R> load(int d, long s) const {
+        const R *b = p + (long)d * 4 * V + s;
+        return Q2<R>{{__ldg(b), __ldg(b + V), __ldg(b + 2 * V), __ldg(b + 3 * V)}};
+    }
+    __device__ __forceinline__ void store(int d, long s, const Q2<R> &m) const {
+        R *b = p + (long)d * 4 * V + s;
+        b[0] = m.e[0]; b[V] = m.e[1]; b[2 * V] = m.e[2]; b[3 * V] = m.e[3];
+    }
+};
+
+template <typename R> struct LinkPlanes<SU3<R>, R> {
+    R *p;
+    long V;
+    __device__ __forceinline__ M3<R> load(int d, long s) const {
+        const R *b = p + (long)d * 18 * V + s;
+        M3<R> m;
+#pragma unroll
+        for (int k = 0; k < 9; k++) { m.r[k] = __ldg(b + k * V); m.i[k] = __ldg(b + (9 + k) * V); }
+        return m;
+    }
+    __device__ __forceinline__ void store(int d, long s, const M3<R> &m) const {
+        R *b = p + (long)d * 18 * V + s;
+#pragma unroll
+        for (int k = 0; k < 9; k++) { b[k * V] = m.r[k]; b[(9 + k) * V] = m.i[k]; }
+    }
+};
+
+// Algebra-valued link field E[d][a][s] (or site field with d = 0).
+template <int NA, typename R> struct AlgPlanes {
+    R *p;
+    long V;
+    __device__ __forceinline__ void load(int d, long s, R *x) const {
+        const R *b = p + (long)d * NA * V + s;
+#pragma unroll
+        for (int a = 0; a < NA; a++) x[a] = b[a * V];
+    }
+    __device__ __forceinline__ void load_ro(int d, long s, R *x) const {
+        const R *b = p + (long)d * NA * V + s;
+#pragma unroll
+        for (int a = 0; a < NA; a++) x[a] = __ldg(b + a * V);
+    }
+    __device__ __forceinline__ void store(int d, long s, const R *x) const {
+        R *b = p + (long)d * NA * V + s;
+#pragma unroll
+        for (int a = 0; a < NA; a++) b[a * V] = x[a];
+    }
+};
+
+}  // namespace opx

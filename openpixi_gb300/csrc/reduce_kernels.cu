@@ -1,0 +1,268 @@
+// reduce_kernels.cu -- whole-lattice reductions and per-cell diagnostics.
+//
+//   k_bulk_partial / k_bulk_final : FieldMeasurements E^2, B^2, Gauss, rho^2
+//       (physics/measurements/FieldMeasurements.java:68-231) as used by
+//       BulkQuantitiesInTime.calculate (diagnostics/methods/BulkQuantitiesInTime.java:83-121).
+//       One pass computes all of them (the reference makes six lattice passes).
+//       Per-site values are formed in the storage precision and accumulated in
+//       FP64 with compensated (Neumaier/TwoSum) sums; the block partials are
+//       combined by one block in a fixed order, so results are deterministic.
+//   k_energy_density   : EnergyDensity.ComponentComputation (EnergyDensity.java:119-166)
+//   k_projected_energy : ProjectedEnergyDensity.EnergyDensityComputation (:114-179)
+//   k_gauss_field      : Grid.getGaussConstraint (Grid.java:944-968) at every cell
+#include "internal.h"
+#include "ksum.cuh"
+
+namespace opx {
+
+// B_d(x) = proj(P_jk(x)) a_d / (a_j a_k) with (d, j, k) cyclic (Grid.getB, Grid.java:901-920)
+template <class G, typename R>
+__device__ __forceinline__ void field_b(const LinkPlanes<G, R> &Up, const Lat &L, long s, const Nbr &nb,
+                                        int d, R *b) {
+    const int j = (d + 1) % 3, k = (d + 2) % 3;
+    // U_j(x) U_k(x+j) U_j(x+k)^dagger U_k(x)^dagger (Grid.getPlaquette, Grid.java:609-642)
+    auto P = G::mul_adj(G::mul_adj(G::mul(Up.load(j, s), Up.load(k, nb.fwd[j])), Up.load(j, nb.fwd[k])),
+                        Up.load(k, s));
+    G::proj(P, b);
+    const R f = R(L.a[d] / (L.a[j] * L.a[k]));
+#pragma unroll
+    for (int a = 0; a < G::NA; a++) b[a] *= f;
+}
+
+// G(x) = sum_i [E_i(x) - U_i(x-i)^dagger E_i(x-i) U_i(x-i)] / (a_i g a_i) - rho(x)
+template <class G, typename R>
+__device__ __forceinline__ void gauss_site(const LinkPlanes<G, R> &Up, const AlgPlanes<G::NA, R> &Ep,
+                                           const R *rho, const Lat &L, long s, const Nbr &nb, R *gs) {
+    constexpr int NA = G::NA;
+#pragma unroll
+    for (int a = 0; a < NA; a++) gs[a] = R(0);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        R e0[NA], e1[NA], t[NA];
+        Ep.load_ro(i, s, e0);
+        Ep.load_ro(i, nb.bwd[i], e1);
+        G::act(e1, G::adj(Up.load(i, nb.bwd[i])), t);
+        const R f = R(1.0 / (L.a[i] * (L.g * L.a[i])));
+#pragma unroll
+        for (int a = 0; a < NA; a++) gs[a] += (e0[a] - t[a]) * f;
+    }
+    if (rho) {
+#pragma unroll
+        for (int a = 0; a < NA; a++) gs[a] -= __ldg(rho + (long)a * L.V + s);
+    }
+}
+
+template <typename R, int NA>
+__device__ __forceinline__ double sq(const R *x) {
+    double s = 0.0;
+#pragma unroll
+    for (int a = 0; a < NA; a++) s += (double)x[a] * (double)x[a];
+    return s;
+}
+
+constexpr int NQ = 8;  // E2[3], B2[3], G2, rho2
+
+template <int NC, typename R>
+__global__ void __launch_bounds__(256) k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext,
+                                                      const R *__restrict__ E, const R *__restrict__ rho,
+                                                      const uint8_t *__restrict__ eval, Lat L,
+                                                      double *__restrict__ part) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+    KSum acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) acc[q] = KSum{0.0, 0.0};
+    double uf[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) uf[i] = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
+    for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < L.V; s += (long)gridDim.x * blockDim.x) {
+        if (eval && !eval[s]) continue;
+        int x[3];
+        site_coords(L, s, x);
+        const Nbr nb = neighbours(L, s, x);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            R e[NA];
+            Ep.load_ro(i, s, e);
+            two_sum_add(acc[i], sq<R, NA>(e) * uf[i]);
+            R b0[NA], b1[NA];
+            field_b<G, R>(Up, L, s, nb, i, b0);
+            field_b<G, R>(Unp, L, s, nb, i, b1);
+            two_sum_add(acc[3 + i], 0.5 * (sq<R, NA>(b0) + sq<R, NA>(b1)) * uf[i]);
+        }
+        R gs[NA];
+        gauss_site<G, R>(Up, Ep, rho, L, s, nb, gs);
+        two_sum_add(acc[6], sq<R, NA>(gs));
+        if (rho) {
+            R r[NA];
+#pragma unroll
+            for (int a = 0; a < NA; a++) r[a] = __ldg(rho + (long)a * L.V + s);
+            two_sum_add(acc[7], sq<R, NA>(r));
+        }
+    }
+    // block reduction: warp shuffles then shared memory, fixed order
+    int q;
+    KSum v = block_reduce<NQ>(acc, q);
+    if (q >= 0) {
+        part[((long)blockIdx.x * NQ + q) * 2] = v.s;
+        part[((long)blockIdx.x * NQ + q) * 2 + 1] = v.c;
+    }
+}
+
+__global__ void k_bulk_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
+    // one thread per quantity, blocks summed in index order
+    const int q = threadIdx.x;
+    if (q >= NQ) return;
+    KSum v{0.0, 0.0};
+    for (int b = 0; b < nblocks; b++) ksum_merge(v, KSum{part[((long)b * NQ + q) * 2], part[((long)b * NQ + q) * 2 + 1]});
+    out[q] = v.s + v.c;
+}
+
+template <int NC, typename R>
+static void bulk_t(Ctx &c) {
+    const int B = 256;
+    k_bulk_partial<NC, R><<<c.red_blocks, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
+                                                            (const R *)c.rho, c.eval, c.L, c.red_part);
+    k_bulk_final<<<1, 32, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
+    c.launches += 2;
+}
+
+void launch_bulk(Ctx &c) {
+    if (c.nc == 2) {
+        if (c.prec == OPX_F64) bulk_t<2, double>(c); else bulk_t<2, float>(c);
+    } else {
+        if (c.prec == OPX_F64) bulk_t<3, double>(c); else bulk_t<3, float>(c);
+    }
+}
+
+// EnergyDensity: sum_d [0.5 E_d^2 + 0.25 (B_d(U) + B_d(Unext))^2] / (g a_0)^2
+// (the direction-0 unit factor for every d and B summed before squaring, as the
+// reference does: EnergyDensity.java:136,154-158)
+template <int NC, typename R>
+__global__ void k_energy_density(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
+                                 const uint8_t *__restrict__ eval, Lat L, double *__restrict__ out) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    if (eval && !eval[s]) { out[s] = 0.0; return; }
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+    int x[3];
+    site_coords(L, s, x);
+    const Nbr nb = neighbours(L, s, x);
+    const double uf = 1.0 / ((L.g * L.a[0]) * (L.g * L.a[0]));
+    double en = 0.0;
+    for (int d = 0; d < 3; d++) {
+        R e[NA], b0[NA], b1[NA];
+        Ep.load_ro(d, s, e);
+        field_b<G, R>(Up, L, s, nb, d, b0);
+        field_b<G, R>(Unp, L, s, nb, d, b1);
+#pragma unroll
+        for (int a = 0; a < NA; a++) b0[a] += b1[a];
+        en += (0.5 * sq<R, NA>(e) + 0.25 * sq<R, NA>(b0)) * uf;
+    }
+    out[s] = en;
+}
+
+// One block per slice x_dir = k; four sums T_el, T_mag, L_el, L_mag.
+template <int NC, typename R>
+__global__ void __launch_bounds__(256) k_projected_energy(const R *__restrict__ U, const R *__restrict__ Unext,
+                                                          const R *__restrict__ E, const uint8_t *__restrict__ eval,
+                                                          Lat L, int dir, double *__restrict__ out) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+    const int k = blockIdx.x;
+    const int o1 = (dir + 1) % 3, o2 = (dir + 2) % 3;
+    const long nt = L.V / L.n[dir];
+    const double area = (double)L.V / (double)L.n[dir];
+    double uf[3];
+    for (int i = 0; i < 3; i++) uf[i] = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i])) / area;
+    KSum acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    for (long t = threadIdx.x; t < nt; t += blockDim.x) {
+        int x[3];
+        x[dir] = k;
+        const int lo = (o1 > o2) ? o1 : o2, hi = (o1 > o2) ? o2 : o1;  // hi = slower of the two
+        x[lo] = (int)(t % L.n[lo]);
+        x[hi] = (int)(t / L.n[lo]);
+        const long s = x[0] * L.stride[0] + x[1] * L.stride[1] + x[2];
+        if (eval && !eval[s]) continue;
+        const Nbr nb = neighbours(L, s, x);
+        double el_t = 0, el_l = 0, mg_t = 0, mg_l = 0;
+        for (int j = 0; j < 3; j++) {
+            R e[NA], b0[NA], b1[NA];
+            Ep.load_ro(j, s, e);
+            field_b<G, R>(Up, L, s, nb, j, b0);
+            field_b<G, R>(Unp, L, s, nb, j, b1);
+            const double el = 0.5 * sq<R, NA>(e) * uf[j];
+            const double mg = 0.25 * (sq<R, NA>(b0) + sq<R, NA>(b1)) * uf[j];
+            if (j == dir) { el_l += el; mg_l += mg; } else { el_t += el; mg_t += mg; }
+        }
+        two_sum_add(acc[0], el_t);
+        two_sum_add(acc[1], mg_t);
+        two_sum_add(acc[2], el_l);
+        two_sum_add(acc[3], mg_l);
+    }
+    int q;
+    KSum v = block_reduce<4>(acc, q);
+    if (q >= 0) out[(long)q * L.n[dir] + k] = v.s + v.c;
+}
+
+template <int NC, typename R>
+__global__ void k_gauss_field(const R *__restrict__ U, const R *__restrict__ E, const R *__restrict__ rho, Lat L,
+                              double *__restrict__ out) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+    int x[3];
+    site_coords(L, s, x);
+    const Nbr nb = neighbours(L, s, x);
+    R gs[NA];
+    gauss_site<G, R>(Up, Ep, rho, L, s, nb, gs);
+#pragma unroll
+    for (int a = 0; a < NA; a++) out[s * NA + a] = (double)gs[a];
+}
+
+#define OPX_DISPATCH(fn, ...)                                              \
+    do {                                                                   \
+        if (c.nc == 2) {                                                   \
+            if (c.prec == OPX_F64) fn<2, double>(__VA_ARGS__);             \
+            else fn<2, float>(__VA_ARGS__);                                \
+        } else {                                                           \
+            if (c.prec == OPX_F64) fn<3, double>(__VA_ARGS__);             \
+            else fn<3, float>(__VA_ARGS__);                                \
+        }                                                                  \
+    } while (0)
+
+template <int NC, typename R>
+static void energy_density_t(Ctx &c, double *out) {
+    k_energy_density<NC, R><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
+                                                                        (const R *)c.E, c.eval, c.L, out);
+    c.launches++;
+}
+void launch_energy_density(Ctx &c, double *out) { OPX_DISPATCH(energy_density_t, c, out); }
+
+template <int NC, typename R>
+static void projected_energy_t(Ctx &c, int dir, double *out) {
+    k_projected_energy<NC, R><<<c.L.n[dir], 256, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
+                                                                (const R *)c.E, c.eval, c.L, dir, out);
+    c.launches++;
+}
+void launch_projected_energy(Ctx &c, int dir, double *out) { OPX_DISPATCH(projected_energy_t, c, dir, out); }
+
+template <int NC, typename R>
+static void gauss_field_t(Ctx &c, double *out) {
+    k_gauss_field<NC, R><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>((const R *)c.U, (const R *)c.E,
+                                                                     (const R *)c.rho, c.L, out);
+    c.launches++;
+}
+void launch_gauss_field(Ctx &c, double *out) { OPX_DISPATCH(gauss_field_t, c, out); }
+
+}  // namespace opx

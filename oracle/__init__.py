@@ -193,6 +193,10 @@ class OracleGrid:
         lib().orc_update_grid_omp(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),
                                   _p(self.active), int(nthreads))
 
+    def update_grid_range_omp(self, s0, s1, nthreads):
+        lib().orc_update_grid_range_omp(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),
+                                        _p(self.active), C.c_long(s0), C.c_long(s1), int(nthreads))
+
     def store_fields(self):
         # Cell.reassignLinks: swap U and Unext (physics/grid/Cell.java:173-177)
         self.U, self.Unext = self.Unext, self.U
@@ -224,6 +228,11 @@ class OracleGrid:
         for m in range(self.V * 3):
             L.orc_gen_to_alg(self.nc, _p(gen[m]), _p(tmp))
             L.orc_alg_getlink(self.nc, _p(tmp), _p(U[m]))
+
+    def random_fields(self, seed, sigma_a, sigma_e):
+        """random_links(seed, sigma_a) and random_e(seed, sigma_e) in one C loop."""
+        lib().orc_random_fields(self.pp, C.c_uint64(seed), C.c_double(sigma_a), C.c_double(sigma_e),
+                                _p(self.U), _p(self.E))
 
     def random_e(self, seed, sigma, stream=1):
         k = ngen(self.nc)

@@ -550,6 +550,18 @@ void orc_update_grid_omp(const orc_params *p, const double *U, double *E, const 
     (void)nthreads;
 }
 
+/* The same over the site range [s0, s1) (a bounded sample of a large lattice). */
+void orc_update_grid_range_omp(const orc_params *p, const double *U, double *E, const double *J,
+                               double *Unext, const uint8_t *active, long s0, long s1, int nthreads)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (long x = s0; x < s1; x++)
+        if (!active || active[x]) combined_update_site(p, U, E, J, Unext, x);
+    (void)nthreads;
+}
+
 int orc_max_threads(void)
 {
 #ifdef _OPENMP
@@ -852,6 +864,28 @@ void orc_random_gen(uint64_t seed, uint64_t stream, long count, double sigma, do
 {
     uint64_t base = stream << 40;
     for (long k = 0; k < count; k++) out[k] = sigma * orc_normal(seed, base + (uint64_t)k);
+}
+
+/* Seeded links U = getLink(A) and fields E (reference layout) for a whole lattice:
+ * the loops of OracleGrid.random_links / random_e done in C for large lattices. */
+void orc_random_fields(const orc_params *p, uint64_t seed, double sigma_a, double sigma_e,
+                       double *U, double *E)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc), k = nc == 3 ? 8 : 3;
+    long n = vol(p) * 3;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (long m = 0; m < n; m++) {
+        double ga[8], ge[8], alg[NA_MAX];
+        for (int a = 0; a < k; a++) {
+            ga[a] = sigma_a * orc_normal(seed, (0ULL << 40) + (uint64_t)(m * k + a));
+            ge[a] = sigma_e * orc_normal(seed, (1ULL << 40) + (uint64_t)(m * k + a));
+        }
+        orc_gen_to_alg(nc, ga, alg);
+        orc_alg_getlink(nc, alg, U + m * ng);
+        orc_gen_to_alg(nc, ge, E + m * na);
+    }
 }
 
 /* div E (x) = sum_i c_i [E_i(x) - Ad(U_i(x-i)^dagger) E_i(x-i)], c_i = 1/(a_i g a_i):

@@ -82,6 +82,8 @@ void orc_update_links(const orc_params *p, const double *U, const double *E,
 /* Same algorithm split over host threads (OpenMP); timed CPU baseline only. */
 void orc_update_grid_omp(const orc_params *p, const double *U, double *E, const double *J,
                          double *Unext, const uint8_t *active, int nthreads);
+void orc_update_grid_range_omp(const orc_params *p, const double *U, double *E, const double *J,
+                               double *Unext, const uint8_t *active, long s0, long s1, int nthreads);
 int orc_max_threads(void);
 
 /* ---- reductions (FieldMeasurements / BulkQuantitiesInTime) ----
@@ -123,6 +125,8 @@ void orc_ngp(const orc_params *p, const double *pos, int32_t *cell3);
 /* ---- seeded synthetic initial conditions ---- */
 double orc_normal(uint64_t seed, uint64_t ctr);
 void orc_random_gen(uint64_t seed, uint64_t stream, long count, double sigma, double *out);
+void orc_random_fields(const orc_params *p, uint64_t seed, double sigma_a, double sigma_e,
+                       double *U, double *E);
 /* Covariant Gauss projection by conjugate gradients on div(divT mu) = rho - div E.
  * Returns iterations used; *final_g2 = mean G^2 afterwards. */
 int orc_gauss_project_cg(const orc_params *p, const double *U, double *E, const double *rho,
