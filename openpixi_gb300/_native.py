@@ -234,7 +234,8 @@ class Handle:
         return out
 
     def projected_energy(self, d):
-        out = np.empty(4 * self.dims[d])
+        # an invalid direction is passed through so that the library reports it
+        out = np.empty(4 * self.dims[d] if 0 <= int(d) < 3 else 1)
         self.check(self.L.opx_projected_energy(self.h, int(d), ptr(out), out.size))
         return out.reshape(4, self.dims[d])
 

@@ -19,10 +19,18 @@ namespace opx {
 
 int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 
+// Register and instruction budget: the SU(3) products are unrolled (108 FMA
+// each) but the loops over the link direction i and the staple plane j stay
+// rolled, with runtime indices resolved by selects, so that the kernel body
+// fits the instruction cache and a thread keeps one staple in flight.
+template <int NC, typename R> struct UpdateBounds { static constexpr int minb = 4; };
+template <> struct UpdateBounds<3, float> { static constexpr int minb = 4; };
+template <> struct UpdateBounds<3, double> { static constexpr int minb = 3; };
+
 template <int NC, typename R, bool HAS_J, bool REUNIT>
-__global__ void __launch_bounds__(128) k_update_grid(const R *__restrict__ U, R *__restrict__ E,
-                                                     const R *__restrict__ J, R *__restrict__ Unext,
-                                                     const uint8_t *__restrict__ active, Lat L) {
+__global__ void __launch_bounds__(128, UpdateBounds<NC, R>::minb)
+k_update_grid(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ J, R *__restrict__ Unext,
+              const uint8_t *__restrict__ active, Lat L) {
     using G = typename GroupOf<NC, R>::T;
     using M = typename G::M;
     constexpr int NA = G::NA;
@@ -31,39 +39,44 @@ __global__ void __launch_bounds__(128) k_update_grid(const R *__restrict__ U, R 
     if (active && !active[s]) return;  // Cell.isActive gate (FastTYMSolver.java:51)
     int x[3];
     site_coords(L, s, x);
-    const Nbr nb = neighbours(L, s, x);
+    const int x0 = x[0], x1 = x[1], x2 = x[2];
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
     const LinkPlanes<G, R> Un{Unext, L.V};
     const AlgPlanes<NA, R> Ep{E, L.V};
     const AlgPlanes<NA, R> Jp{const_cast<R *>(J), L.V};
     const R dt = R(L.dt);
 
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < 3; i++) {
+        const int xi = pick(x0, x1, x2, i);
+        const long s_pi = shift_d(L, s, xi, i, +1);  // x + i
         M S = G::zero();
-#pragma unroll
+#pragma unroll 1
         for (int jj = 1; jj < 3; jj++) {
-            const int j = (i + jj) % 3;
+            const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
+            const int xj = pick(x0, x1, x2, j);
+            const long s_pj = shift_d(L, s, xj, j, +1);     // x + j
+            const long s_mj = shift_d(L, s, xj, j, -1);     // x - j
+            const long s_pimj = shift_d(L, s_pi, xj, j, -1);  // x + i - j
             // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
-            M F = G::mul_adj(G::mul_adj(Up.load(j, nb.fwd[i]), Up.load(i, nb.fwd[j])), Up.load(j, s));
+            M F = G::mul_adj(G::mul_adj(Up.load(j, s_pi), Up.load(i, s_pj)), Up.load(j, s));
             // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
-            const long sij = nb.fwd[i] + (nb.bwd[j] - s);
-            const M C = G::mul(Up.load(i, nb.bwd[j]), Up.load(j, sij));
-            G::add(F, G::adj_mul(C, Up.load(j, nb.bwd[j])));
-            G::scale(F, R(1.0 / (L.a[j] * L.a[j])));
+            const M C = G::mul(Up.load(i, s_mj), Up.load(j, s_pimj));
+            G::add(F, G::adj_mul(C, Up.load(j, s_mj)));
+            const R aj = R(pickd(L.a[0], L.a[1], L.a[2], j));
+            G::scale(F, R(1) / (aj * aj));
             G::add(S, F);
         }
         const M Ui = Up.load(i, s);
-        const M P = G::mul(Ui, S);
         R pr[NA], e[NA];
-        G::proj(P, pr);
+        G::proj(G::mul(Ui, S), pr);
         Ep.load(i, s, e);
 #pragma unroll
         for (int a = 0; a < NA; a++) e[a] += pr[a] * dt;
         if (HAS_J) {
             R jv[NA];
             Jp.load_ro(i, s, jv);
-            const R jf = R(-(L.g * L.a[i]) * L.dt);
+            const R jf = R(-(L.g * pickd(L.a[0], L.a[1], L.a[2], i)) * L.dt);
 #pragma unroll
             for (int a = 0; a < NA; a++) e[a] += jv[a] * jf;
         }

@@ -62,6 +62,18 @@ __device__ __forceinline__ Nbr neighbours(const Lat &L, long s, const int *x) {
     return nb;
 }
 
+// Shift by one unit in direction d (runtime) with orientation o, given the
+// coordinate xd of s along d.  Selects instead of indexed arrays keep
+// everything in registers when d is not a compile-time constant.
+__device__ __forceinline__ long shift_d(const Lat &L, long s, int xd, int d, int o) {
+    const int nd = d == 0 ? L.n[0] : (d == 1 ? L.n[1] : L.n[2]);
+    const long st = d == 0 ? L.stride[0] : (d == 1 ? L.stride[1] : 1L);
+    if (o > 0) return xd == nd - 1 ? s - (long)(nd - 1) * st : s + st;
+    return xd == 0 ? s + (long)(nd - 1) * st : s - st;
+}
+__device__ __forceinline__ int pick(int a0, int a1, int a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
+__device__ __forceinline__ double pickd(double a0, double a1, double a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
+
 // Structure-of-arrays views
 template <class G, typename R> struct LinkPlanes {
     R *p;

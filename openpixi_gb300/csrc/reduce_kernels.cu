@@ -12,96 +12,17 @@
 //   k_gauss_field      : Grid.getGaussConstraint (Grid.java:944-968) at every cell
 #include "internal.h"
 #include "ksum.cuh"
+#include "observables.cuh"
 
 namespace opx {
-
-// B_d(x) = proj(P_jk(x)) a_d / (a_j a_k) with (d, j, k) cyclic (Grid.getB, Grid.java:901-920)
-template <class G, typename R>
-__device__ __forceinline__ void field_b(const LinkPlanes<G, R> &Up, const Lat &L, long s, const Nbr &nb,
-                                        int d, R *b) {
-    const int j = (d + 1) % 3, k = (d + 2) % 3;
-    // U_j(x) U_k(x+j) U_j(x+k)^dagger U_k(x)^dagger (Grid.getPlaquette, Grid.java:609-642)
-    auto P = G::mul_adj(G::mul_adj(G::mul(Up.load(j, s), Up.load(k, nb.fwd[j])), Up.load(j, nb.fwd[k])),
-                        Up.load(k, s));
-    G::proj(P, b);
-    const R f = R(L.a[d] / (L.a[j] * L.a[k]));
-#pragma unroll
-    for (int a = 0; a < G::NA; a++) b[a] *= f;
-}
-
-// G(x) = sum_i [E_i(x) - U_i(x-i)^dagger E_i(x-i) U_i(x-i)] / (a_i g a_i) - rho(x)
-template <class G, typename R>
-__device__ __forceinline__ void gauss_site(const LinkPlanes<G, R> &Up, const AlgPlanes<G::NA, R> &Ep,
-                                           const R *rho, const Lat &L, long s, const Nbr &nb, R *gs) {
-    constexpr int NA = G::NA;
-#pragma unroll
-    for (int a = 0; a < NA; a++) gs[a] = R(0);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        R e0[NA], e1[NA], t[NA];
-        Ep.load_ro(i, s, e0);
-        Ep.load_ro(i, nb.bwd[i], e1);
-        G::act(e1, G::adj(Up.load(i, nb.bwd[i])), t);
-        const R f = R(1.0 / (L.a[i] * (L.g * L.a[i])));
-#pragma unroll
-        for (int a = 0; a < NA; a++) gs[a] += (e0[a] - t[a]) * f;
-    }
-    if (rho) {
-#pragma unroll
-        for (int a = 0; a < NA; a++) gs[a] -= __ldg(rho + (long)a * L.V + s);
-    }
-}
-
-template <typename R, int NA>
-__device__ __forceinline__ double sq(const R *x) {
-    double s = 0.0;
-#pragma unroll
-    for (int a = 0; a < NA; a++) s += (double)x[a] * (double)x[a];
-    return s;
-}
-
-constexpr int NQ = 8;  // E2[3], B2[3], G2, rho2
 
 template <int NC, typename R>
 __global__ void __launch_bounds__(256) k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext,
                                                       const R *__restrict__ E, const R *__restrict__ rho,
                                                       const uint8_t *__restrict__ eval, Lat L,
                                                       double *__restrict__ part) {
-    using G = typename GroupOf<NC, R>::T;
-    constexpr int NA = G::NA;
-    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
-    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
     KSum acc[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; q++) acc[q] = KSum{0.0, 0.0};
-    double uf[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) uf[i] = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
-    for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < L.V; s += (long)gridDim.x * blockDim.x) {
-        if (eval && !eval[s]) continue;
-        int x[3];
-        site_coords(L, s, x);
-        const Nbr nb = neighbours(L, s, x);
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            R e[NA];
-            Ep.load_ro(i, s, e);
-            two_sum_add(acc[i], sq<R, NA>(e) * uf[i]);
-            R b0[NA], b1[NA];
-            field_b<G, R>(Up, L, s, nb, i, b0);
-            field_b<G, R>(Unp, L, s, nb, i, b1);
-            two_sum_add(acc[3 + i], 0.5 * (sq<R, NA>(b0) + sq<R, NA>(b1)) * uf[i]);
-        }
-        R gs[NA];
-        gauss_site<G, R>(Up, Ep, rho, L, s, nb, gs);
-        two_sum_add(acc[6], sq<R, NA>(gs));
-        if (rho) {
-            R r[NA];
-#pragma unroll
-            for (int a = 0; a < NA; a++) r[a] = __ldg(rho + (long)a * L.V + s);
-            two_sum_add(acc[7], sq<R, NA>(r));
-        }
-    }
+    bulk_accumulate<NC, R>(U, Unext, E, rho, eval, L, acc);
     // block reduction: warp shuffles then shared memory, fixed order
     int q;
     KSum v = block_reduce<NQ>(acc, q);
