@@ -1,0 +1,191 @@
+"""Diagnostics: host-side mirror of diagnostics/Diagnostics.java and the methods
+of this path.  The numbers come from the device reductions (opx_reduce,
+opx_energy_density, opx_projected_energy); these classes only schedule them and
+write the reference's file formats.
+
+  BulkQuantitiesInTime   diagnostics/methods/BulkQuantitiesInTime.java (TSV, :66, :83-121)
+  EnergyDensity          diagnostics/methods/EnergyDensity.java (big-endian binary, :15-31, :119-166)
+  ProjectedEnergyDensity diagnostics/methods/ProjectedEnergyDensity.java (TSV rows, :91-105, :114-179)
+"""
+import decimal
+import os
+import struct
+import time
+
+import numpy as np
+
+_D = decimal.Context(prec=17, rounding=decimal.ROUND_HALF_EVEN)
+
+
+def java_sci(x):
+    """java.text.DecimalFormat("0.################E0").format(x): one integer
+    digit, up to 16 fraction digits (HALF_EVEN), no '+' in the exponent."""
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return ("-" if x < 0 else "") + "∞"
+    if x == 0.0:
+        return ("-" if str(x).startswith("-") else "") + "0E0"
+    d = _D.create_decimal(x)
+    sign, digits, exp = d.as_tuple()
+    ds = "".join(str(v) for v in digits).rstrip("0") or "0"
+    e10 = exp + len(digits) - 1
+    mant = ds[0] + ("." + ds[1:] if len(ds) > 1 else "")
+    return ("-" if sign else "") + mant + "E" + str(e10)
+
+
+def java_double(x):
+    """Double.toString for the time column of ProjectedEnergyDensity."""
+    x = float(x)
+    if x == 0.0:
+        return "0.0"
+    ax = abs(x)
+    if 1e-3 <= ax < 1e7:
+        r = repr(x)
+        return r if "." in r or "e" in r else r + ".0"
+    m, e = repr(x).split("e") if "e" in repr(x) else (None, None)
+    if m is None:
+        s = "%.17e" % x
+        m, e = s.split("e")
+        m = m.rstrip("0")
+    if "." not in m:
+        m += ".0"
+    return f"{m}E{int(e)}"
+
+
+class Diagnostics:
+    """diagnostics/Diagnostics.java:32-51"""
+
+    def initialize(self, simulation):
+        raise NotImplementedError
+
+    def calculate(self, grid, particles, steps):
+        raise NotImplementedError
+
+
+class BulkQuantitiesInTime(Diagnostics):
+    HEADER = "#time \t E^2 \t B^2 \t P_x \t P_y \t P_z \t G \t rho^2"
+
+    def __init__(self, path, time_interval, supress_output=False):
+        self.path = path
+        self.timeInterval = float(time_interval)
+        self.supressOutput = supress_output
+        self.rows = []
+
+    def initialize(self, s):
+        self.s = s
+        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        if not self.supressOutput:
+            with open(self.path, "w") as f:
+                f.write(self.HEADER + "\n")
+
+    def calculate(self, grid, particles, steps):
+        if steps % self.stepInterval != 0:
+            return
+        o = grid.reduce()
+        self.eSquared, self.bSquared = o.e2_total, o.b2_total
+        self.px, self.py, self.pz = o.px, o.py, o.pz
+        self.gaussViolation, self.totalChargeSquared = o.gauss, o.rho2
+        row = [steps * self.s.getTimeStep(), o.e2_total, o.b2_total, o.px, o.py, o.pz, o.gauss, o.rho2]
+        self.rows.append(row)
+        if not self.supressOutput:
+            with open(self.path, "a") as f:
+                f.write("\t".join(java_sci(v) for v in row) + "\n")
+
+
+class EnergyDensity(Diagnostics):
+    """Per-cell energy density, one big-endian binary file per output time:
+    int32 D, int32 N[D], then V float64 (Java DataOutputStream)."""
+
+    def __init__(self, filename, start_time, time_interval):
+        self.filename = filename
+        self.startTime = float(start_time)
+        self.timeInterval = float(time_interval)
+        self.counter = 0
+        self.last = None
+
+    def initialize(self, s):
+        self.firstStep = int(max(round(self.startTime / s.getTimeStep()), 1))
+        self.step = int(round(self.timeInterval / s.getTimeStep()))
+        self.s = s
+
+    def calculate(self, grid, particles, steps):
+        if steps % self.step != 0 or steps < self.firstStep:
+            return
+        self.counter += 1
+        base, ext = os.path.splitext(self.filename)
+        path = f"{base}_{self.counter}{ext}"
+        e = grid.energy_density()
+        self.last = e
+        with open(path, "wb") as f:
+            f.write(struct.pack(">i", 3))
+            f.write(struct.pack(">3i", *grid.dims))
+            f.write(e.astype(">f8").tobytes())
+
+
+class ProjectedEnergyDensity(Diagnostics):
+    def __init__(self, path, time_interval, direction, compute_energy_density=True,
+                 compute_poynting_vector=False):
+        self.path = path
+        self.timeInterval = float(time_interval)
+        self.direction = int(direction)
+        self.computeEnergyDensity = compute_energy_density
+        self.computePoyntingVector = compute_poynting_vector
+        if compute_poynting_vector:
+            raise NotImplementedError("ProjectedEnergyDensity: the Poynting vector rows are not provided")
+        self.last = None
+
+    def initialize(self, s):
+        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        open(self.path, "w").close()
+
+    def calculate(self, grid, particles, steps):
+        if steps % self.stepInterval != 0:
+            return
+        rows = grid.projected_energy(self.direction) if self.computeEnergyDensity else None
+        self.last = rows
+        with open(self.path, "a") as f:
+            f.write(java_double(steps * grid.getTemporalSpacing()) + "\n")
+            if rows is not None:
+                for r in rows:
+                    f.write("\t".join(java_sci(v) for v in r) + "\n")
+
+
+class TimeMeasurement(Diagnostics):
+    """diagnostics/methods/TimeMeasurement.java: wall time per output interval."""
+
+    def __init__(self, path, interval):
+        self.path = path
+        self.interval = float(interval)
+
+    def initialize(self, s):
+        self.stepInterval = int(max(round(self.interval / s.getTimeStep()), 1))
+        self.t0 = time.perf_counter()
+        open(self.path, "w").close()
+
+    def calculate(self, grid, particles, steps):
+        if steps % self.stepInterval != 0:
+            return
+        grid.synchronize()
+        with open(self.path, "a") as f:
+            f.write(f"{steps}\t{time.perf_counter() - self.t0:.6f}\n")
+
+
+def from_yaml(out):
+    """YamlOutput.applyTo (ui/util/yaml/YamlOutput.java) for the outputs of this path."""
+    ds = []
+    for o in out.get("bulkQuantitiesInTime") or []:
+        ds.append(BulkQuantitiesInTime(o["path"], o["interval"]))
+    for o in out.get("energyDensity") or []:
+        ds.append(EnergyDensity(o["path"], o.get("startTime", 0.0), o["timeInterval"]))
+    for o in out.get("projectedEnergyDensity") or []:
+        ds.append(ProjectedEnergyDensity(o["path"], o["interval"], o.get("direction", 0),
+                                         o.get("computeEnergyDensity", True),
+                                         o.get("computePoyntingVector", True)))
+    for o in out.get("timeMeasurement") or []:
+        ds.append(TimeMeasurement(o["path"], o["interval"]))
+    unsupported = set(out) - {"bulkQuantitiesInTime", "energyDensity", "projectedEnergyDensity", "timeMeasurement"}
+    if unsupported:
+        raise NotImplementedError(f"output generators not provided: {sorted(unsupported)}")
+    return ds
