@@ -176,6 +176,26 @@ int opx_time_steps(opx_ctx *ctx, int nsteps, double *ms);
 /* Number of kernels this handle has launched since creation. */
 long opx_kernel_launches(const opx_ctx *ctx);
 
+/* Allocation-free BulkQuantities reductions over caller-owned device fields
+ * (no counterpart in the reference).  For callers that cannot allocate device
+ * memory themselves or through this library: hosts whose device memory is
+ * owned by another allocator (a framework's caching allocator, a JVM or
+ * service with a fixed GPU budget) or code that must not stall on the device
+ * synchronisation of cudaMalloc/cudaFree.  Computes what opx_reduce computes
+ * and writes one opx_observables record to out_device (device memory), queued
+ * on `stream` (a cudaStream_t; NULL = the default stream).  Fields are device
+ * pointers in the handle's structure-of-arrays layout: U, Unext [3][ng][V],
+ * E [3][ngen][V], rho [ngen][V] (NULL = zero charge), eval [V] (NULL = all
+ * cells), elements double (OPX_F64) or float (OPX_F32).
+ * Calls no cudaMalloc/cudaFree: its scratch is a fixed 77,824-byte __device__
+ * array of the library, held by every GPU that loads the library until exit.
+ * Limit: V <= 2^29 sites (larger lattices return OPX_ERR_INVALID).  The first
+ * call on a device looks up the scratch address and should come before any
+ * stream capture.  Calls share the scratch, so calls that overlap on the GPU race. */
+int opx_reduce_noalloc(int ncolors, int precision, const int *dims, const double *a, double g,
+                       const void *U, const void *Unext, const void *E, const void *rho,
+                       const uint8_t *eval, opx_observables *out_device, void *stream);
+
 /* Page-locked host memory for transfers (cudaMallocHost / cudaFreeHost). */
 void *opx_host_alloc(size_t bytes);
 void opx_host_free(void *p);

@@ -36,7 +36,7 @@ EXPORTED = [
     "opx_particles_upload", "opx_particles_download", "opx_cpic_phases",
     "opx_init_random", "opx_gauss_project",
     "opx_set_profiling", "opx_phase_times", "opx_time_steps", "opx_kernel_launches",
-    "opx_host_alloc", "opx_host_free",
+    "opx_host_alloc", "opx_host_free", "opx_reduce_noalloc",
 ]
 
 
@@ -114,6 +114,8 @@ def load(path=None):
         "opx_kernel_launches": (C.c_long, [vp]),
         "opx_host_alloc": (vp, [sz]),
         "opx_host_free": (None, [vp]),
+        "opx_reduce_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                         C.c_double, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

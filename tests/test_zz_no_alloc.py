@@ -1,0 +1,77 @@
+"""opx_reduce_noalloc: the reductions for callers that cannot allocate device
+memory (their device memory belongs to another allocator, or they must not stall
+on cudaMalloc).  The caller owns every device buffer -- here torch tensors stand
+in for such a caller's memory -- and the entry point uses only the library's
+fixed static scratch.  Its output must equal opx_reduce's (relative 1e-12) on
+two calls in a row, since every call reuses the same scratch.
+
+This file is collected last so that a stopped run has already run the others.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import openpixi_gb300 as opx
+from openpixi_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("e2", "b2", "px", "py", "pz", "gauss", "rho2", "e2_total", "b2_total")
+
+
+def as_vec(o):
+    return np.array(list(o.e2) + list(o.b2) + [o.px, o.py, o.pz, o.gauss, o.rho2, o.e2_total, o.b2_total])
+
+
+def planes(arr, ndir):
+    """Host [V][ndir][k] -> device layout [ndir][k][V] (contiguous)."""
+    V = arr.shape[0]
+    if ndir == 0:
+        return np.ascontiguousarray(arr.T)
+    return np.ascontiguousarray(arr.transpose(1, 2, 0)).reshape(-1, V)
+
+
+@pytest.mark.parametrize("nc,prec", [(3, N.OPX_F32), (2, N.OPX_F64)])
+def test_noalloc_matches_reduce(native, nc, prec):
+    torch = pytest.importorskip("torch")
+    dims = (12, 10, 14)
+    h = opx.Handle(nc, dims, dt=0.05, precision=prec, reunit_every=10 if prec == N.OPX_F32 else 0)
+    h.init_random(31, 0.3, 0.3)
+    h.gauss_project(1e-24)
+    rng = np.random.default_rng(4)
+    rho = rng.normal(0, 0.05, (h.V, h.ngen))
+    h.upload(N.FIELD_RHO, rho, layout=N.LAYOUT_GEN)
+    h.initialize()
+    h.step(3)
+    ref = as_vec(h.reduce())
+
+    dt = torch.float32 if prec == N.OPX_F32 else torch.float64
+    dev = torch.device("cuda", 0)
+    U = torch.from_numpy(planes(h.download(N.FIELD_U), 3)).to(dev, dt)
+    Un = torch.from_numpy(planes(h.download(N.FIELD_UNEXT), 3)).to(dev, dt)
+    E = torch.from_numpy(planes(h.download(N.FIELD_E, layout=N.LAYOUT_GEN), 3)).to(dev, dt)
+    R = torch.from_numpy(planes(h.download(N.FIELD_RHO, layout=N.LAYOUT_GEN), 0)).to(dev, dt)
+    out = torch.full((13,), float("nan"), dtype=torch.float64, device=dev)
+    dims_c = (C.c_int * 3)(*dims)
+    a_c = (C.c_double * 3)(1.0, 1.0, 1.0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for _ in range(2):
+        out.fill_(float("nan"))
+        rc = native.opx_reduce_noalloc(nc, prec, dims_c, a_c, 1.0, C.c_void_p(U.data_ptr()),
+                                       C.c_void_p(Un.data_ptr()), C.c_void_p(E.data_ptr()),
+                                       C.c_void_p(R.data_ptr()), None, C.c_void_p(out.data_ptr()),
+                                       C.c_void_p(stream))
+        assert rc == N.OPX_OK
+        torch.cuda.synchronize(dev)
+        got = out.cpu().numpy()
+        assert np.all(np.isfinite(got))
+        assert np.allclose(got, ref, rtol=1e-12, atol=1e-300), (got, ref)
+
+
+def test_noalloc_rejects_oversize(native):
+    dims_c = (C.c_int * 3)(1024, 1024, 1024)
+    a_c = (C.c_double * 3)(1.0, 1.0, 1.0)
+    rc = native.opx_reduce_noalloc(2, N.OPX_F64, dims_c, a_c, 1.0, C.c_void_p(8), C.c_void_p(8),
+                                   C.c_void_p(8), None, None, C.c_void_p(8), None)
+    assert rc == N.OPX_ERR_INVALID
