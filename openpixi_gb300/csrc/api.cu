@@ -20,6 +20,8 @@ struct opx_ctx {
 
 static std::string g_create_error;
 
+Ctx &opx::ctx_of(opx_ctx *h) { return h->c; }
+
 #define API_CHECK(ctx)                                   \
     do {                                                 \
         if (!(ctx)) return OPX_ERR_INVALID;              \
@@ -45,16 +47,15 @@ static int sync_check(Ctx &c, const char *where) {
 
 template <typename R>
 __global__ void k_fill_identity(R *U, long V, int ng, int nc) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over 3*ng*V
-    if (t >= 3L * ng * V) return;
-    const long plane = t / V;
-    const int c = (int)(plane % ng);
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over the blocked link array
+    if (t >= link_elems(V, ng)) return;
+    const int c = (int)((t >> 5) % ng);
     const bool one = nc == 3 ? (c == 0 || c == 4 || c == 8) : (c == 0);
     U[t] = one ? R(1) : R(0);
 }
 
 static void fill_identity(Ctx &c, void *U) {
-    const long n = 3L * c.ng * c.L.V;
+    const long n = link_elems(c.L.V, c.ng);
     if (c.prec == OPX_F64) k_fill_identity<double><<<grid_for(n, 256), 256, 0, c.stream>>>((double *)U, c.L.V, c.ng, c.nc);
     else k_fill_identity<float><<<grid_for(n, 256), 256, 0, c.stream>>>((float *)U, c.L.V, c.ng, c.nc);
     c.launches++;
@@ -109,7 +110,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     c.rsize = c.prec == OPX_F64 ? 8 : 4;
     bool ok = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) == cudaSuccess;
     auto al = [&](void **p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) { ok = false; *p = nullptr; } };
-    const size_t nU = (size_t)V * 3 * c.ng, nE = (size_t)V * 3 * c.na;
+    const size_t nU = (size_t)link_elems(V, c.ng), nE = (size_t)V * 3 * c.na;
     al(&c.U, nU * c.rsize);
     al(&c.Unext, nU * c.rsize);
     al(&c.E, nE * c.rsize);

@@ -17,7 +17,7 @@ __global__ void k_links_from_ref(const double *__restrict__ src, R *__restrict__
     if (t >= V * 3) return;
     const long s = t / 3;
     const int d = (int)(t - s * 3);
-    for (int c = 0; c < ng; c++) dst[((long)d * ng + c) * V + s] = (R)src[t * ng + c];
+    for (int c = 0; c < ng; c++) dst[link_offset(V, ng, d, c, s)] = (R)src[t * ng + c];
 }
 
 template <typename R>
@@ -26,7 +26,7 @@ __global__ void k_links_to_ref(const R *__restrict__ src, double *__restrict__ d
     if (t >= V * 3) return;
     const long s = t / 3;
     const int d = (int)(t - s * 3);
-    for (int c = 0; c < ng; c++) dst[t * ng + c] = (double)src[((long)d * ng + c) * V + s];
+    for (int c = 0; c < ng; c++) dst[t * ng + c] = (double)src[link_offset(V, ng, d, c, s)];
 }
 
 // SU3AlgebraElement.get(j)

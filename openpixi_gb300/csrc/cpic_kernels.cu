@@ -148,7 +148,7 @@ __global__ void k_cpic_push(Particles P, const double *__restrict__ Unext, Lat L
         // update uses U^dagger, i.e. Unext(old)^dagger or Unext(new).
         double Uadj[NG], U[NG];
         const long cl = P.vel[d * n + k] > 0 ? cell_old : cell_new;
-        for (int c = 0; c < NG; c++) U[c] = Unext[((long)d * NG + c) * L.V + cl];
+        for (int c = 0; c < NG; c++) U[c] = Unext[link_offset(L.V, NG, d, c, cl)];
         if (vel[d] > 0) {
             if (NC == 3) ref_su3_adj(U, Uadj);
             else { Uadj[0] = U[0]; Uadj[1] = -U[1]; Uadj[2] = -U[2]; Uadj[3] = -U[3]; }

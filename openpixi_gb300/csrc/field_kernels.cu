@@ -7,108 +7,40 @@
 //   k_update_links: FastTYMSolver.UpdateLinks (:65-84): Unext = exp(-i dt E) U
 //   k_reunit      : re-unitarisation of FP32 links (no counterpart in the reference)
 //
-// One thread owns one site and updates its three links, so U_i(x) and the
+// The per-site arithmetic is in leapfrog.cuh.  One thread owns one site and updates its three links, so U_i(x) and the
 // site's own links are read once and reused for all staples.  Compulsory HBM
 // traffic per link update: read U_i(x), E_i(x) [, J_i(x)], write E_i(x),
 // Unext_i(x); the 12 neighbour links of the staples are served from L1/L2
 // (consecutive blocks cover consecutive sites, so the +-1 planes of dimension
 // 0 are resident in L2 while a block works on its plane).
 #include "internal.h"
+#include "leapfrog.cuh"
 
 namespace opx {
 
 int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 
-// Register and instruction budget: the SU(3) products are unrolled (108 FMA
-// each) but the loops over the link direction i and the staple plane j stay
-// rolled, with runtime indices resolved by selects, so that the kernel body
-// fits the instruction cache and a thread keeps one staple in flight.
 template <int NC, typename R> struct UpdateBounds { static constexpr int minb = 4; };
-template <> struct UpdateBounds<3, float> { static constexpr int minb = 4; };
 template <> struct UpdateBounds<3, double> { static constexpr int minb = 3; };
 
 template <int NC, typename R, bool HAS_J, bool REUNIT>
 __global__ void __launch_bounds__(128, UpdateBounds<NC, R>::minb)
 k_update_grid(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ J, R *__restrict__ Unext,
               const uint8_t *__restrict__ active, Lat L) {
-    using G = typename GroupOf<NC, R>::T;
-    using M = typename G::M;
-    constexpr int NA = G::NA;
     const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.V) return;
     if (active && !active[s]) return;  // Cell.isActive gate (FastTYMSolver.java:51)
-    int x[3];
-    site_coords(L, s, x);
-    const int x0 = x[0], x1 = x[1], x2 = x[2];
-    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
-    const LinkPlanes<G, R> Un{Unext, L.V};
-    const AlgPlanes<NA, R> Ep{E, L.V};
-    const AlgPlanes<NA, R> Jp{const_cast<R *>(J), L.V};
-    const R dt = R(L.dt);
-
-#pragma unroll 1
-    for (int i = 0; i < 3; i++) {
-        const int xi = pick(x0, x1, x2, i);
-        const long s_pi = shift_d(L, s, xi, i, +1);  // x + i
-        M S = G::zero();
-#pragma unroll 1
-        for (int jj = 1; jj < 3; jj++) {
-            const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
-            const int xj = pick(x0, x1, x2, j);
-            const long s_pj = shift_d(L, s, xj, j, +1);     // x + j
-            const long s_mj = shift_d(L, s, xj, j, -1);     // x - j
-            const long s_pimj = shift_d(L, s_pi, xj, j, -1);  // x + i - j
-            // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
-            M F = G::mul_adj(G::mul_adj(Up.load(j, s_pi), Up.load(i, s_pj)), Up.load(j, s));
-            // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
-            const M C = G::mul(Up.load(i, s_mj), Up.load(j, s_pimj));
-            G::add(F, G::adj_mul(C, Up.load(j, s_mj)));
-            const R aj = R(pickd(L.a[0], L.a[1], L.a[2], j));
-            G::scale(F, R(1) / (aj * aj));
-            G::add(S, F);
-        }
-        const M Ui = Up.load(i, s);
-        R pr[NA], e[NA];
-        G::proj(G::mul(Ui, S), pr);
-        Ep.load(i, s, e);
-#pragma unroll
-        for (int a = 0; a < NA; a++) e[a] += pr[a] * dt;
-        if (HAS_J) {
-            R jv[NA];
-            Jp.load_ro(i, s, jv);
-            const R jf = R(-(L.g * pickd(L.a[0], L.a[1], L.a[2], i)) * L.dt);
-#pragma unroll
-            for (int a = 0; a < NA; a++) e[a] += jv[a] * jf;
-        }
-        Ep.store(i, s, e);
-        R v[NA];
-#pragma unroll
-        for (int a = 0; a < NA; a++) v[a] = -dt * e[a];
-        M Vn = G::mul(G::expi(v), Ui);
-        if (REUNIT) G::reunit(Vn);
-        Un.store(i, s, Vn);
-    }
+    update_site<NC, R, HAS_J, REUNIT>(U, E, J, Unext, L, s);
 }
 
 template <int NC, typename R>
 __global__ void __launch_bounds__(128) k_update_links(const R *__restrict__ U, const R *__restrict__ E,
                                                       R *__restrict__ Unext, const uint8_t *__restrict__ active,
                                                       Lat L) {
-    using G = typename GroupOf<NC, R>::T;
-    constexpr int NA = G::NA;
     const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.V) return;
     if (active && !active[s]) return;
-    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
-    const LinkPlanes<G, R> Un{Unext, L.V};
-    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
-    for (int k = 0; k < 3; k++) {
-        R e[NA], v[NA];
-        Ep.load_ro(k, s, e);
-#pragma unroll
-        for (int a = 0; a < NA; a++) v[a] = -R(L.dt) * e[a];
-        Un.store(k, s, G::mul(G::expi(v), Up.load(k, s)));
-    }
+    update_links_site<NC, R>(U, E, Unext, L, s);
 }
 
 template <int NC, typename R>

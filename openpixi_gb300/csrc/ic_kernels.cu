@@ -175,7 +175,7 @@ struct Dot {
 
 int ic_init_random(Ctx &c, uint64_t seed, double sigma_a, double sigma_e) {
     const long V = c.L.V;
-    const size_t nU = (size_t)V * 3 * c.ng, nE = (size_t)V * 3 * c.na;
+    const size_t nU = (size_t)link_elems(V, c.ng), nE = (size_t)V * 3 * c.na;
     double *U64 = nullptr, *E64 = nullptr;
     const bool f32 = c.prec == OPX_F32;
     if (f32) {
@@ -207,7 +207,7 @@ int ic_gauss_project(Ctx &c, double tol, int maxit, int *iters, double *final_g2
     const long V = c.L.V;
     const int NA = c.na;
     const long ns = V * NA, nl = ns * 3;
-    const size_t nU = (size_t)V * 3 * c.ng;
+    const size_t nU = (size_t)link_elems(V, c.ng);
     const bool f32 = c.prec == OPX_F32;
     std::vector<double *> bufs;
     auto alloc = [&](size_t n) -> double * {

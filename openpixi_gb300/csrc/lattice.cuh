@@ -2,12 +2,15 @@
 //
 // Site index s = ((x0*N1)+x1)*N2+x2, dimension 0 slowest (Grid.java:757-770),
 // so dimension 2 is contiguous and a warp reads 32 consecutive sites.
-// Fields are stored as planes: component c of direction d of every site is a
-// contiguous array of V values,
-//   links  U[d][c][s]  (c < NG: 4 for SU(2), 18 for SU(3))
+// Links are stored in warp-sized blocks of 32 consecutive sites,
+//   U[d][s/32][c][s%32]   (c < NG: 4 for SU(2), 18 for SU(3)),
+// so that component c of 32 consecutive sites is one 128-byte (FP32) or
+// 256-byte (FP64) line, and the NG components of one link sit at fixed
+// 32-element strides from one address (one address computation per link).
+// Algebra fields are plain planes, one contiguous array of V values per
+// component:
 //   fields E[d][a][s]  (a < NA: 3 for SU(2), 8 for SU(3), generator components)
 //   rho    [a][s]
-// which makes every per-component access of a thread block fully coalesced.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -22,6 +25,10 @@ struct Lat {
     long stride[3];  // n1*n2, n2, 1
     double a[3];
     double dt, g;
+    // the staple area factors 1/a_j^2 and current factors -g a_i dt, in both
+    // precisions, so that FP32 kernels do no FP64 arithmetic or conversions
+    double inva2[3], jfac[3];
+    float inva2f[3], jfacf[3], dtf;
 };
 
 __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double g) {
@@ -33,8 +40,35 @@ __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double
     L.stride[0] = (long)dims[1] * dims[2];
     L.dt = dt;
     L.g = g;
+    for (int i = 0; i < 3; i++) {
+        L.inva2[i] = 1.0 / (a[i] * a[i]);
+        L.jfac[i] = -(g * a[i]) * dt;
+        L.inva2f[i] = (float)L.inva2[i];
+        L.jfacf[i] = (float)L.jfac[i];
+    }
+    L.dtf = (float)dt;
     return L;
 }
+
+template <typename R> struct LatR;
+template <> struct LatR<double> {
+    __device__ __forceinline__ static double inva2(const Lat &L, int d) {
+        return d == 0 ? L.inva2[0] : (d == 1 ? L.inva2[1] : L.inva2[2]);
+    }
+    __device__ __forceinline__ static double jfac(const Lat &L, int d) {
+        return d == 0 ? L.jfac[0] : (d == 1 ? L.jfac[1] : L.jfac[2]);
+    }
+    __device__ __forceinline__ static double dt(const Lat &L) { return L.dt; }
+};
+template <> struct LatR<float> {
+    __device__ __forceinline__ static float inva2(const Lat &L, int d) {
+        return d == 0 ? L.inva2f[0] : (d == 1 ? L.inva2f[1] : L.inva2f[2]);
+    }
+    __device__ __forceinline__ static float jfac(const Lat &L, int d) {
+        return d == 0 ? L.jfacf[0] : (d == 1 ? L.jfacf[1] : L.jfacf[2]);
+    }
+    __device__ __forceinline__ static float dt(const Lat &L) { return L.dtf; }
+};
 
 // Periodic neighbour offsets of site s (Grid.shift, Grid.java:802-823).
 struct Nbr {
@@ -74,6 +108,13 @@ __device__ __forceinline__ long shift_d(const Lat &L, long s, int xd, int d, int
 __device__ __forceinline__ int pick(int a0, int a1, int a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
 __device__ __forceinline__ double pickd(double a0, double a1, double a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
 
+// Warp-blocked link layout
+__host__ __device__ __forceinline__ long link_blocks(long V) { return (V + 31) >> 5; }
+__host__ __device__ __forceinline__ long link_offset(long V, int NG, int d, int c, long s) {
+    return (((long)d * link_blocks(V) + (s >> 5)) * NG + c) * 32 + (s & 31);
+}
+__host__ __device__ __forceinline__ long link_elems(long V, int NG) { return 3L * link_blocks(V) * 32 * NG; }
+
 // Structure-of-arrays views
 template <class G, typename R> struct LinkPlanes {
     R *p;
@@ -86,12 +127,12 @@ template <typename R> struct LinkPlanes<SU2<R>, R> {
     R *p;
     long V;
     __device__ __forceinline__ Q2<R> load(int d, long s) const {
-        const R *b = p + (long)d * 4 * V + s;
-        return Q2<R>{{__ldg(b), __ldg(b + V), __ldg(b + 2 * V), __ldg(b + 3 * V)}};
+        const R *b = p + link_offset(V, 4, d, 0, s);
+        return Q2<R>{{__ldg(b), __ldg(b + 32), __ldg(b + 64), __ldg(b + 96)}};
     }
     __device__ __forceinline__ void store(int d, long s, const Q2<R> &m) const {
-        R *b = p + (long)d * 4 * V + s;
-        b[0] = m.e[0]; b[V] = m.e[1]; b[2 * V] = m.e[2]; b[3 * V] = m.e[3];
+        R *b = p + link_offset(V, 4, d, 0, s);
+        b[0] = m.e[0]; b[32] = m.e[1]; b[64] = m.e[2]; b[96] = m.e[3];
     }
 };
 
@@ -99,16 +140,16 @@ template <typename R> struct LinkPlanes<SU3<R>, R> {
     R *p;
     long V;
     __device__ __forceinline__ M3<R> load(int d, long s) const {
-        const R *b = p + (long)d * 18 * V + s;
+        const R *b = p + link_offset(V, 18, d, 0, s);
         M3<R> m;
 #pragma unroll
-        for (int k = 0; k < 9; k++) { m.r[k] = __ldg(b + k * V); m.i[k] = __ldg(b + (9 + k) * V); }
+        for (int k = 0; k < 9; k++) { m.r[k] = __ldg(b + k * 32); m.i[k] = __ldg(b + (9 + k) * 32); }
         return m;
     }
     __device__ __forceinline__ void store(int d, long s, const M3<R> &m) const {
-        R *b = p + (long)d * 18 * V + s;
+        R *b = p + link_offset(V, 18, d, 0, s);
 #pragma unroll
-        for (int k = 0; k < 9; k++) { b[k * V] = m.r[k]; b[(9 + k) * V] = m.i[k]; }
+        for (int k = 0; k < 9; k++) { b[k * 32] = m.r[k]; b[(9 + k) * 32] = m.i[k]; }
     }
 };
 

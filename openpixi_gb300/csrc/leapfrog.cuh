@@ -1,0 +1,96 @@
+// leapfrog.cuh -- one site of the temporal-gauge leapfrog, shared by the
+// single-lattice kernel (field_kernels.cu) and the batched persistent kernel
+// (batch_kernels.cu).
+//
+// FastTYMSolver.CombinedUpdate (physics/fields/FastTYMSolver.java:40-63) with
+// Grid.getStapleSum (physics/grid/Grid.java:675-696):
+//     E_i(x) += dt proj(U_i(x) S_i(x)) - g a_i dt J_i(x)
+//     Unext_i(x) = exp(-i dt E_i(x)) U_i(x)
+//
+// Register and instruction budget: the SU(3) products are unrolled (108 FMA
+// each) but the loops over the link direction i and the staple plane j stay
+// rolled, with runtime indices resolved by selects, so that the body fits the
+// instruction cache and a thread keeps one staple in flight.
+#pragma once
+#include "lattice.cuh"
+
+namespace opx {
+
+template <int NC, typename R, bool HAS_J, bool REUNIT>
+__device__ __forceinline__ void update_site(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ J,
+                                            R *__restrict__ Unext, const Lat &L, long s) {
+    using G = typename GroupOf<NC, R>::T;
+    using M = typename G::M;
+    constexpr int NA = G::NA;
+    int x[3];
+    site_coords(L, s, x);
+    const int x0 = x[0], x1 = x[1], x2 = x[2];
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
+    const LinkPlanes<G, R> Un{Unext, L.V};
+    const AlgPlanes<NA, R> Ep{E, L.V};
+    const AlgPlanes<NA, R> Jp{const_cast<R *>(J), L.V};
+    const R dt = LatR<R>::dt(L);
+
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) {
+        const int xi = pick(x0, x1, x2, i);
+        const long s_pi = shift_d(L, s, xi, i, +1);  // x + i
+        M S = G::zero();
+#pragma unroll 1
+        for (int jj = 1; jj < 3; jj++) {
+            const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
+            const int xj = pick(x0, x1, x2, j);
+            const long s_pj = shift_d(L, s, xj, j, +1);       // x + j
+            const long s_mj = shift_d(L, s, xj, j, -1);       // x - j
+            const long s_pimj = shift_d(L, s_pi, xj, j, -1);  // x + i - j
+            // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
+            M F = G::mul_adj(G::mul_adj(Up.load(j, s_pi), Up.load(i, s_pj)), Up.load(j, s));
+            // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
+            const M C = G::mul(Up.load(i, s_mj), Up.load(j, s_pimj));
+            G::add(F, G::adj_mul(C, Up.load(j, s_mj)));
+            G::scale(F, LatR<R>::inva2(L, j));
+            G::add(S, F);
+        }
+        const M Ui = Up.load(i, s);
+        R pr[NA], e[NA];
+        G::proj(G::mul(Ui, S), pr);
+        Ep.load(i, s, e);
+#pragma unroll
+        for (int a = 0; a < NA; a++) e[a] += pr[a] * dt;
+        if (HAS_J) {
+            R jv[NA];
+            Jp.load_ro(i, s, jv);
+            const R jf = LatR<R>::jfac(L, i);
+#pragma unroll
+            for (int a = 0; a < NA; a++) e[a] += jv[a] * jf;
+        }
+        Ep.store(i, s, e);
+        R v[NA];
+#pragma unroll
+        for (int a = 0; a < NA; a++) v[a] = -dt * e[a];
+        M Vn = G::mul(G::expi(v), Ui);
+        if (REUNIT) G::reunit(Vn);
+        Un.store(i, s, Vn);
+    }
+}
+
+// FastTYMSolver.UpdateLinks (:65-84): Unext = exp(-i dt E) U at one site
+template <int NC, typename R>
+__device__ __forceinline__ void update_links_site(const R *__restrict__ U, const R *__restrict__ E,
+                                                  R *__restrict__ Unext, const Lat &L, long s) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
+    const LinkPlanes<G, R> Un{Unext, L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+#pragma unroll 1
+    for (int k = 0; k < 3; k++) {
+        R e[NA], v[NA];
+        Ep.load_ro(k, s, e);
+#pragma unroll
+        for (int a = 0; a < NA; a++) v[a] = -LatR<R>::dt(L) * e[a];
+        Un.store(k, s, G::mul(G::expi(v), Up.load(k, s)));
+    }
+}
+
+}  // namespace opx

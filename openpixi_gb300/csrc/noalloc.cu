@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(256) k_noalloc_partial(const R *__restrict__ U
                                                          const uint8_t *__restrict__ eval, Lat L,
                                                          double *__restrict__ part) {
     KSum acc[NQ];
-    bulk_accumulate<NC, R>(U, Unext, E, rho, eval, L, acc);
+    bulk_accumulate<NC, R>(U, Unext, E, rho, eval, L, acc, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                           (long)gridDim.x * blockDim.x);
     int q;
     KSum v = block_reduce<NQ>(acc, q);
     if (q >= 0) {

@@ -53,13 +53,14 @@ __device__ __forceinline__ double sq(const R *x) {
 
 constexpr int NQ = 8;  // E2[3], B2[3], G2, rho2
 
-// Per-thread compensated sums of the BulkQuantities columns over a grid-stride
-// range of sites (FieldMeasurements EFieldSquared/BFieldSquared/GaussLaw/
+// Per-thread compensated sums of the BulkQuantities columns over the sites
+// first, first + stride, ... (FieldMeasurements EFieldSquared/BFieldSquared/GaussLaw/
 // TotalChargeSquared, physics/measurements/FieldMeasurements.java:68-231).
 template <int NC, typename R>
 __device__ __forceinline__ void bulk_accumulate(const R *__restrict__ U, const R *__restrict__ Unext,
                                                 const R *__restrict__ E, const R *__restrict__ rho,
-                                                const uint8_t *__restrict__ eval, const Lat &L, KSum *acc) {
+                                                const uint8_t *__restrict__ eval, const Lat &L, KSum *acc,
+                                                long first, long stride) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
@@ -69,7 +70,7 @@ __device__ __forceinline__ void bulk_accumulate(const R *__restrict__ U, const R
     double uf[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) uf[i] = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
-    for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < L.V; s += (long)gridDim.x * blockDim.x) {
+    for (long s = first; s < L.V; s += stride) {
         if (eval && !eval[s]) continue;
         int x[3];
         site_coords(L, s, x);

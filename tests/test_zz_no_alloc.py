@@ -25,11 +25,20 @@ def as_vec(o):
 
 
 def planes(arr, ndir):
-    """Host [V][ndir][k] -> device layout [ndir][k][V] (contiguous)."""
+    """Host [V][ndir][k] -> device algebra layout [ndir][k][V] (contiguous)."""
     V = arr.shape[0]
     if ndir == 0:
         return np.ascontiguousarray(arr.T)
     return np.ascontiguousarray(arr.transpose(1, 2, 0)).reshape(-1, V)
+
+
+def link_blocks(arr):
+    """Host links [V][3][ng] -> device layout [3][ceil(V/32)][ng][32]."""
+    V, _, ng = arr.shape
+    nb = (V + 31) // 32
+    pad = np.zeros((nb * 32, 3, ng))
+    pad[:V] = arr
+    return np.ascontiguousarray(pad.reshape(nb, 32, 3, ng).transpose(2, 0, 3, 1))
 
 
 @pytest.mark.parametrize("nc,prec", [(3, N.OPX_F32), (2, N.OPX_F64)])
@@ -48,8 +57,8 @@ def test_noalloc_matches_reduce(native, nc, prec):
 
     dt = torch.float32 if prec == N.OPX_F32 else torch.float64
     dev = torch.device("cuda", 0)
-    U = torch.from_numpy(planes(h.download(N.FIELD_U), 3)).to(dev, dt)
-    Un = torch.from_numpy(planes(h.download(N.FIELD_UNEXT), 3)).to(dev, dt)
+    U = torch.from_numpy(link_blocks(h.download(N.FIELD_U))).to(dev, dt)
+    Un = torch.from_numpy(link_blocks(h.download(N.FIELD_UNEXT))).to(dev, dt)
     E = torch.from_numpy(planes(h.download(N.FIELD_E, layout=N.LAYOUT_GEN), 3)).to(dev, dt)
     R = torch.from_numpy(planes(h.download(N.FIELD_RHO, layout=N.LAYOUT_GEN), 0)).to(dev, dt)
     out = torch.full((13,), float("nan"), dtype=torch.float64, device=dev)
