@@ -245,6 +245,52 @@ def config_for(w, wname):
             else "lattice fits in L2", "parallelism": "replicas (one lattice per GPU)"}
 
 
+def bench_batch(device, nsteps=200, nev=256, seed=SEED):
+    """Batching form: 256 SU(2) events of cubic sizes drawn uniformly from
+    {16,24,32,40,48}^3, FP32 with reunitarisation every 10 steps, 200 steps in
+    one persistent launch replayed from a CUDA graph (autotuned cluster / block
+    size), against the plain FP64 single-lattice path looping over the same
+    events (GPU time of each event's 200 steps, summed)."""
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.choice([16, 24, 32, 40, 48], nev)]
+    dims = [(L, L, L) for L in sizes]
+    b = opx.Batch(2, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
+    b.init_random([seed + 1000 + q for q in range(nev)], 0.1, 0.1, tol=1e-24)
+    b.initialize()
+    cluster, block = b.autotune(steps=5)
+    b.run(nsteps)  # instantiates the graph
+    b.run(nsteps)
+    l0 = b.kernel_launches
+    ms = b.time_run(nsteps)
+    launches = b.kernel_launches - l0
+    links = 3 * sum(L ** 3 for L in sizes)
+    obs = b.reduce()
+    # plain FP64 path, one lattice at a time, same fields
+    handles = {}
+    ms64 = 0.0
+    for q, d in enumerate(dims):
+        h = handles.get(d)
+        if h is None:
+            h = handles[d] = opx.Handle(2, d, dt=0.05, precision=N.OPX_F64, device=device)
+        h.upload(N.FIELD_U, b.download(q, N.FIELD_U))
+        h.upload(N.FIELD_E, b.download(q, N.FIELD_E))
+        h.initialize()
+        ms64 += h.time_steps(nsteps)
+    for h in handles.values():
+        h.close()
+    peak, _ = hbm_peak()
+    lu = links * nsteps / (ms / 1000.0)
+    b.close()
+    return {"events": nev, "steps": nsteps, "lattice_sizes": "L^3, L uniform in {16,24,32,40,48}",
+            "link_updates_per_step": links, "ms": ms, "events_per_s": nev / (ms / 1000.0),
+            "link_updates_per_s": lu, "roofline_frac": 56.0 * lu / 1e9 / peak, "bytes_per_link": 56,
+            "fp64_loop_ms": ms64, "fp64_loop_events_per_s": nev / (ms64 / 1000.0),
+            "speedup_vs_fp64_loop": ms64 / ms, "cluster": cluster, "block": block, "graph": True,
+            "gpu_launches": launches, "max_gauss": max(o.gauss for o in obs)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,6 +300,7 @@ def main():
     ap.add_argument("--workload", default="su3_fp32_128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -355,6 +402,10 @@ def main():
                        "timed region (bytes amortised over the steps); BulkQuantities read back every 10 steps"}
         h2.close()
 
+    batched = None
+    if not args.no_batch and args.workload == "su3_fp32_128":
+        batched = bench_batch(device)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, U_host.array, E_host.array)
@@ -364,7 +415,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": w["prec"], "data": "synthetic",
                 "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
-                "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64,
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64, "batched": batched,
                 "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
                 "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
         print(json.dumps(line), flush=True)

@@ -176,6 +176,36 @@ int opx_time_steps(opx_ctx *ctx, int nsteps, double *ms);
 /* Number of kernels this handle has launched since creation. */
 long opx_kernel_launches(const opx_ctx *ctx);
 
+/* ---- batching form: many independent lattices ("events") in one launch ----
+ * The reference runs one Simulation per event (a loop over independent
+ * Simulation objects); here every event advances in one persistent launch of
+ * thread-block clusters, each cluster owning a load-balanced set of events,
+ * captured in a CUDA graph.  Events are pure Yang-Mills (no particles).
+ * dims: [nevents][3]; a: [nevents][3] lattice spacings or NULL (all 1). */
+typedef struct opx_batch opx_batch;
+int opx_batch_create(int ncolors, int nevents, const int *dims, const double *a, double dt, double g,
+                     int precision, int reunit_every, int device, opx_batch **out);
+void opx_batch_destroy(opx_batch *b);
+const char *opx_batch_last_error(const opx_batch *b);
+/* Seeded Gaussian links / E per event (seeds[nevents]), E projected onto
+ * Gauss's law to mean G^2 <= tol_g2 (tol_g2 <= 0: no projection). */
+int opx_batch_init_random(opx_batch *b, const uint64_t *seeds, double sigma_a, double sigma_e, double tol_g2);
+int opx_batch_upload(opx_batch *b, int event, int field, const double *host, size_t count, int layout);
+int opx_batch_download(opx_batch *b, int event, int field, double *host, size_t count, int layout);
+/* Simulation.initialize (stepLinks) for every event */
+int opx_batch_initialize(opx_batch *b);
+/* Pick the cluster size and block size by timing `steps` steps of each
+ * candidate on the batch itself (the fields are restored afterwards). */
+int opx_batch_autotune(opx_batch *b, int steps, int *cluster, int *block);
+/* nsteps x Simulation.step (no diagnostics) of every event in one launch;
+ * use_graph != 0 replays a captured CUDA graph of that launch. */
+int opx_batch_run(opx_batch *b, int nsteps, int use_graph);
+int opx_batch_time_run(opx_batch *b, int nsteps, int use_graph, double *ms);
+/* BulkQuantities of every event (out[nevents]), FP64 compensated sums */
+int opx_batch_reduce(opx_batch *b, opx_observables *out);
+int opx_batch_config(const opx_batch *b, int *cluster, int *block, int *nclusters);
+long opx_batch_kernel_launches(const opx_batch *b);
+
 /* Allocation-free BulkQuantities reductions over caller-owned device fields
  * (no counterpart in the reference).  For callers that cannot allocate device
  * memory themselves or through this library: hosts whose device memory is
@@ -184,9 +214,10 @@ long opx_kernel_launches(const opx_ctx *ctx);
  * synchronisation of cudaMalloc/cudaFree.  Computes what opx_reduce computes
  * and writes one opx_observables record to out_device (device memory), queued
  * on `stream` (a cudaStream_t; NULL = the default stream).  Fields are device
- * pointers in the handle's structure-of-arrays layout: U, Unext [3][ng][V],
- * E [3][ngen][V], rho [ngen][V] (NULL = zero charge), eval [V] (NULL = all
- * cells), elements double (OPX_F64) or float (OPX_F32).
+ * pointers in the handle's layout: links U, Unext in warp-sized site blocks
+ * [3][ceil(V/32)][ng][32], algebra fields as planes E [3][ngen][V],
+ * rho [ngen][V] (NULL = zero charge), eval [V] (NULL = all cells), elements
+ * double (OPX_F64) or float (OPX_F32).
  * Calls no cudaMalloc/cudaFree: its scratch is a fixed 77,824-byte __device__
  * array of the library, held by every GPU that loads the library until exit.
  * Limit: V <= 2^29 sites (larger lattices return OPX_ERR_INVALID).  The first

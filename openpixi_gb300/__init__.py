@@ -3,8 +3,8 @@
 the C ABI of ``libopixi_gpu.so`` (include/opixi.h), with a host-side mirror of
 the reference's Java API (Settings, Simulation, Grid, FieldSolver,
 Diagnostics, YAML input)."""
-from ._native import (Handle, OpixiError, PinnedArray, OPX_F32, OPX_F64, FIELD_U, FIELD_UNEXT,
+from ._native import (Handle, Batch, OpixiError, PinnedArray, OPX_F32, OPX_F64, FIELD_U, FIELD_UNEXT,
                       FIELD_E, FIELD_J, FIELD_RHO, LAYOUT_REF, LAYOUT_GEN)
 
-__all__ = ["Handle", "OpixiError", "PinnedArray", "OPX_F32", "OPX_F64", "FIELD_U", "FIELD_UNEXT",
+__all__ = ["Handle", "Batch", "OpixiError", "PinnedArray", "OPX_F32", "OPX_F64", "FIELD_U", "FIELD_UNEXT",
            "FIELD_E", "FIELD_J", "FIELD_RHO", "LAYOUT_REF", "LAYOUT_GEN"]

@@ -37,6 +37,10 @@ EXPORTED = [
     "opx_init_random", "opx_gauss_project",
     "opx_set_profiling", "opx_phase_times", "opx_time_steps", "opx_kernel_launches",
     "opx_host_alloc", "opx_host_free", "opx_reduce_noalloc",
+    "opx_batch_create", "opx_batch_destroy", "opx_batch_last_error", "opx_batch_init_random",
+    "opx_batch_upload", "opx_batch_download", "opx_batch_initialize", "opx_batch_autotune",
+    "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
+    "opx_batch_kernel_launches",
 ]
 
 
@@ -114,6 +118,20 @@ def load(path=None):
         "opx_kernel_launches": (C.c_long, [vp]),
         "opx_host_alloc": (vp, [sz]),
         "opx_host_free": (None, [vp]),
+        "opx_batch_create": (C.c_int, [C.c_int, C.c_int, vp, vp, C.c_double, C.c_double, C.c_int, C.c_int,
+                                       C.c_int, C.POINTER(vp)]),
+        "opx_batch_destroy": (None, [vp]),
+        "opx_batch_last_error": (C.c_char_p, [vp]),
+        "opx_batch_init_random": (C.c_int, [vp, vp, C.c_double, C.c_double, C.c_double]),
+        "opx_batch_upload": (C.c_int, [vp, C.c_int, C.c_int, vp, sz, C.c_int]),
+        "opx_batch_download": (C.c_int, [vp, C.c_int, C.c_int, vp, sz, C.c_int]),
+        "opx_batch_initialize": (C.c_int, [vp]),
+        "opx_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "opx_batch_run": (C.c_int, [vp, C.c_int, C.c_int]),
+        "opx_batch_time_run": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "opx_batch_reduce": (C.c_int, [vp, vp]),
+        "opx_batch_config": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "opx_batch_kernel_launches": (C.c_long, [vp]),
         "opx_reduce_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                          C.c_double, vp, vp, vp, vp, vp, vp, vp]),
     }
@@ -298,6 +316,92 @@ class Handle:
     @property
     def kernel_launches(self):
         return self.L.opx_kernel_launches(self.h)
+
+
+class Batch:
+    """Owning wrapper around one ``opx_batch`` (many independent lattices)."""
+
+    def __init__(self, ncolors, dims_list, dt=0.05, g=1.0, precision=OPX_F32, reunit_every=0, device=0,
+                 spacings=None):
+        self.L = load()
+        dims = np.ascontiguousarray(np.asarray(dims_list, dtype=np.int32).reshape(-1, 3))
+        a = None if spacings is None else np.ascontiguousarray(np.asarray(spacings, float).reshape(-1, 3))
+        h = C.c_void_p()
+        rc = self.L.opx_batch_create(int(ncolors), dims.shape[0], ptr(dims), ptr(a), float(dt), float(g),
+                                     int(precision), int(reunit_every), int(device), C.byref(h))
+        if rc != OPX_OK:
+            raise OpixiError(rc, "opx_batch_create failed")
+        self.h = h
+        self.ncolors = int(ncolors)
+        self.dims = [tuple(int(x) for x in d) for d in dims]
+        self.n = dims.shape[0]
+        self.ng = 18 if ncolors == 3 else 4
+        self.na_ref = 9 if ncolors == 3 else 3
+        self.ngen = 8 if ncolors == 3 else 3
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.opx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc != OPX_OK:
+            raise OpixiError(rc, self.L.opx_batch_last_error(self.h).decode())
+        return rc
+
+    def init_random(self, seeds, sigma_a, sigma_e, tol=1e-24):
+        s = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
+        self.check(self.L.opx_batch_init_random(self.h, ptr(s), float(sigma_a), float(sigma_e), float(tol)))
+
+    def _shape(self, q, field, layout):
+        V = int(np.prod(self.dims[q]))
+        na = self.na_ref if layout == LAYOUT_REF else self.ngen
+        return (V, 3, self.ng) if field in (FIELD_U, FIELD_UNEXT) else (V, 3, na)
+
+    def upload(self, q, field, arr, layout=LAYOUT_REF):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self.check(self.L.opx_batch_upload(self.h, int(q), field, ptr(a), a.size, layout))
+
+    def download(self, q, field, layout=LAYOUT_REF):
+        out = np.empty(self._shape(q, field, layout))
+        self.check(self.L.opx_batch_download(self.h, int(q), field, ptr(out), out.size, layout))
+        return out
+
+    def initialize(self):
+        self.check(self.L.opx_batch_initialize(self.h))
+
+    def autotune(self, steps=5):
+        c, b = C.c_int(), C.c_int()
+        self.check(self.L.opx_batch_autotune(self.h, int(steps), C.byref(c), C.byref(b)))
+        return c.value, b.value
+
+    def run(self, nsteps, use_graph=True):
+        self.check(self.L.opx_batch_run(self.h, int(nsteps), 1 if use_graph else 0))
+
+    def time_run(self, nsteps, use_graph=True):
+        ms = C.c_double()
+        self.check(self.L.opx_batch_time_run(self.h, int(nsteps), 1 if use_graph else 0, C.byref(ms)))
+        return ms.value
+
+    def reduce(self):
+        out = (Observables * self.n)()
+        self.check(self.L.opx_batch_reduce(self.h, out))
+        return list(out)
+
+    def config(self):
+        c, b, n = C.c_int(), C.c_int(), C.c_int()
+        self.check(self.L.opx_batch_config(self.h, C.byref(c), C.byref(b), C.byref(n)))
+        return {"cluster": c.value, "block": b.value, "clusters": n.value}
+
+    @property
+    def kernel_launches(self):
+        return self.L.opx_batch_kernel_launches(self.h)
 
 
 class PinnedArray:

@@ -84,4 +84,7 @@ void launch_cpic_phases(Ctx &c, int reassign);
 
 int grid_for(long n, int block);
 
+// the handle behind an opx_ctx (api.cu)
+Ctx &ctx_of(opx_ctx *h);
+
 }  // namespace opx

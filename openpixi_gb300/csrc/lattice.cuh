@@ -108,6 +108,12 @@ __device__ __forceinline__ long shift_d(const Lat &L, long s, int xd, int d, int
 __device__ __forceinline__ int pick(int a0, int a1, int a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
 __device__ __forceinline__ double pickd(double a0, double a1, double a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
 
+// Read-only loads through the non-coherent cache for built-in element types;
+// other element types (the dual numbers of the tangent-linear form) load plainly.
+template <typename R> __device__ __forceinline__ R ld(const R *p) { return *p; }
+template <> __device__ __forceinline__ float ld<float>(const float *p) { return __ldg(p); }
+template <> __device__ __forceinline__ double ld<double>(const double *p) { return __ldg(p); }
+
 // Warp-blocked link layout
 __host__ __device__ __forceinline__ long link_blocks(long V) { return (V + 31) >> 5; }
 __host__ __device__ __forceinline__ long link_offset(long V, int NG, int d, int c, long s) {
@@ -128,7 +134,7 @@ template <typename R> struct LinkPlanes<SU2<R>, R> {
     long V;
     __device__ __forceinline__ Q2<R> load(int d, long s) const {
         const R *b = p + link_offset(V, 4, d, 0, s);
-        return Q2<R>{{__ldg(b), __ldg(b + 32), __ldg(b + 64), __ldg(b + 96)}};
+        return Q2<R>{{ld(b), ld(b + 32), ld(b + 64), ld(b + 96)}};
     }
     __device__ __forceinline__ void store(int d, long s, const Q2<R> &m) const {
         R *b = p + link_offset(V, 4, d, 0, s);
@@ -143,7 +149,7 @@ template <typename R> struct LinkPlanes<SU3<R>, R> {
         const R *b = p + link_offset(V, 18, d, 0, s);
         M3<R> m;
 #pragma unroll
-        for (int k = 0; k < 9; k++) { m.r[k] = __ldg(b + k * 32); m.i[k] = __ldg(b + (9 + k) * 32); }
+        for (int k = 0; k < 9; k++) { m.r[k] = ld(b + k * 32); m.i[k] = ld(b + (9 + k) * 32); }
         return m;
     }
     __device__ __forceinline__ void store(int d, long s, const M3<R> &m) const {
@@ -165,7 +171,7 @@ template <int NA, typename R> struct AlgPlanes {
     __device__ __forceinline__ void load_ro(int d, long s, R *x) const {
         const R *b = p + (long)d * NA * V + s;
 #pragma unroll
-        for (int a = 0; a < NA; a++) x[a] = __ldg(b + a * V);
+        for (int a = 0; a < NA; a++) x[a] = ld(b + a * V);
     }
     __device__ __forceinline__ void store(int d, long s, const R *x) const {
         R *b = p + (long)d * NA * V + s;
