@@ -154,10 +154,35 @@ int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count);
  *             physics/movement/solver/CGCParticleSolver.java) ---- */
 int opx_particles_upload(opx_ctx *ctx, const opx_particles *p);
 int opx_particles_download(opx_ctx *ctx, opx_particles *p);
+/* Number of particles attached to the handle (s.particles.size()). */
+long opx_particles_count(const opx_ctx *ctx);
 /* Particle phases of one Simulation.step (reassign != 0) or of
  * Simulation.initialize (reassign == 0): charge density, positions, transport,
  * charges, currents (Simulation.java:398-421, 329-347). */
 int opx_cpic_phases(opx_ctx *ctx, int reassign);
+
+/* ---- CGC initial conditions (physics/initial/CGC/CGCInitialCondition.java:55-93) ----
+ * One MV-model nucleus (MVModel.java constructor arguments, YAML keys of
+ * ui/util/yaml/initial/YamlMVModel.java). */
+typedef struct {
+    int direction;       /* beam axis (0) */
+    int orientation;     /* +1 or -1 */
+    double location;     /* longitudinalLocation */
+    double width;        /* longitudinalWidth */
+    double mu;           /* MV parameter mu */
+    int use_seed;        /* randomSeed given */
+    int seed;            /* java.util.Random seed */
+    double uvt;          /* ultravioletCutoffTransverse */
+    double coherence;    /* longitudinalCoherenceLength */
+    double ir;           /* infraredCoefficient */
+} opx_mv_nucleus;
+/* Applies the nuclei in order: MV charges (java.util.Random stream), 3D
+ * momentum-space regulation and 2D Poisson solves (cuFFT), Wilson lines,
+ * links U and Unext (improved, M = 20), E from the temporal plaquette, and the
+ * NGP particles of LightConeNGPParticleCreator (round(aL/dt) per cell, 100+100
+ * refinement sweeps), which are attached to the handle.  OPX_F64 handles,
+ * beam along direction 0.  Call opx_initialize afterwards (Simulation.initialize). */
+int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
 
 /* ---- seeded synthetic initial conditions (no counterpart in the reference) ---- */
 /* U_i(x) = exp(i A_i^a(x) t_a), A ~ N(0, sigma_a^2); E_i^a(x) ~ N(0, sigma_e^2);
@@ -175,6 +200,25 @@ int opx_phase_times(opx_ctx *ctx, double *ms, long *counts, int nphases);
 int opx_time_steps(opx_ctx *ctx, int nsteps, double *ms);
 /* Number of kernels this handle has launched since creation. */
 long opx_kernel_launches(const opx_ctx *ctx);
+
+/* ---- differentiation form (SU(2); no counterpart in the reference) ----
+ * Objective J = mean over the box lo..hi (inclusive cell coordinates; NULL =
+ * whole lattice) of the per-cell energy density of
+ * EnergyDensity.ComponentComputation (diagnostics/methods/EnergyDensity.java:119-166)
+ * after nsteps x Simulation.step from the handle's current U and E (as
+ * before opx_initialize).  The handle's fields are not modified.
+ * Host direction / gradient arrays: [V][3][3] generator components of E. */
+/* J at E + h*dE (dE may be NULL), from an FP64 forward run: finite differences */
+int opx_energy_objective(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double h,
+                         double *J);
+/* FP64 tangent-linear run: J and dJ along dE (the forward kernels on dual numbers) */
+int opx_energy_tangent(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double *J,
+                       double *dJ);
+/* Adjoint: dJ/dE_0 for every link.  The forward runs in the handle's precision
+ * with FP64 checkpoints every ckpt steps (about sqrt(nsteps)); the reverse
+ * sweep recomputes each segment in FP64 and applies the reverse step. */
+int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const int *hi, double *J,
+                        double *grad, size_t count);
 
 /* ---- batching form: many independent lattices ("events") in one launch ----
  * The reference runs one Simulation per event (a loop over independent

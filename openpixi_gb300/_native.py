@@ -41,6 +41,8 @@ EXPORTED = [
     "opx_batch_upload", "opx_batch_download", "opx_batch_initialize", "opx_batch_autotune",
     "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
     "opx_batch_kernel_launches",
+    "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
+    "opx_particles_count",
 ]
 
 
@@ -65,6 +67,12 @@ class Observables(C.Structure):
         return {"e2": list(self.e2), "b2": list(self.b2), "px": self.px, "py": self.py, "pz": self.pz,
                 "gauss": self.gauss, "rho2": self.rho2, "e2_total": self.e2_total,
                 "b2_total": self.b2_total}
+
+
+class MVNucleus(C.Structure):
+    _fields_ = [("direction", C.c_int), ("orientation", C.c_int), ("location", C.c_double),
+                ("width", C.c_double), ("mu", C.c_double), ("use_seed", C.c_int), ("seed", C.c_int),
+                ("uvt", C.c_double), ("coherence", C.c_double), ("ir", C.c_double)]
 
 
 class Particles(C.Structure):
@@ -132,6 +140,11 @@ def load(path=None):
         "opx_batch_reduce": (C.c_int, [vp, vp]),
         "opx_batch_config": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "opx_batch_kernel_launches": (C.c_long, [vp]),
+        "opx_cgc_mv": (C.c_int, [vp, vp, C.c_int]),
+        "opx_particles_count": (C.c_long, [vp]),
+        "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
+        "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
+        "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
         "opx_reduce_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                          C.c_double, vp, vp, vp, vp, vp, vp, vp]),
     }
@@ -297,6 +310,44 @@ class Handle:
         g2 = C.c_double()
         self.check(self.L.opx_gauss_project(self.h, float(tol), int(maxit), C.byref(it), C.byref(g2)))
         return it.value, g2.value
+
+    # ---- CGC initial conditions ----
+    def cgc_mv(self, nuclei):
+        """nuclei: list of dicts with the MVNucleus fields."""
+        arr = (MVNucleus * len(nuclei))()
+        for k, nu in enumerate(nuclei):
+            for f, _ in MVNucleus._fields_:
+                setattr(arr[k], f, nu[f])
+        self.check(self.L.opx_cgc_mv(self.h, arr, len(nuclei)))
+        self.np = self.L.opx_particles_count(self.h)
+
+    # ---- differentiation form (SU(2)) ----
+    @staticmethod
+    def _box(lo, hi):
+        lo_c = None if lo is None else (C.c_int * 3)(*[int(v) for v in lo])
+        hi_c = None if hi is None else (C.c_int * 3)(*[int(v) for v in hi])
+        return lo_c, hi_c
+
+    def energy_objective(self, nsteps, lo=None, hi=None, dE=None, h=0.0):
+        lo_c, hi_c = self._box(lo, hi)
+        d = None if dE is None else np.ascontiguousarray(dE, dtype=np.float64)
+        J = C.c_double()
+        self.check(self.L.opx_energy_objective(self.h, int(nsteps), lo_c, hi_c, ptr(d), float(h), C.byref(J)))
+        return J.value
+
+    def energy_tangent(self, nsteps, dE, lo=None, hi=None):
+        lo_c, hi_c = self._box(lo, hi)
+        d = np.ascontiguousarray(dE, dtype=np.float64)
+        J, dJ = C.c_double(), C.c_double()
+        self.check(self.L.opx_energy_tangent(self.h, int(nsteps), lo_c, hi_c, ptr(d), C.byref(J), C.byref(dJ)))
+        return J.value, dJ.value
+
+    def energy_gradient(self, nsteps, ckpt, lo=None, hi=None):
+        lo_c, hi_c = self._box(lo, hi)
+        g = np.empty((self.V, 3, self.ngen))
+        J = C.c_double()
+        self.check(self.L.opx_energy_gradient(self.h, int(nsteps), int(ckpt), lo_c, hi_c, C.byref(J), ptr(g), g.size))
+        return J.value, g
 
     # ---- timing ----
     def set_profiling(self, on=True):

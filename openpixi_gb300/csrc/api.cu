@@ -502,6 +502,8 @@ int opx_particles_download(opx_ctx *ctx, opx_particles *p) {
     return OPX_OK;
 }
 
+long opx_particles_count(const opx_ctx *ctx) { return ctx ? ctx->c.P.n : -1; }
+
 int opx_init_random(opx_ctx *ctx, uint64_t seed, double sigma_a, double sigma_e) {
     API_CHECK(ctx);
     Ctx &c = ctx->c;
