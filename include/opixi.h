@@ -180,8 +180,10 @@ typedef struct {
  * momentum-space regulation and 2D Poisson solves (cuFFT), Wilson lines,
  * links U and Unext (improved, M = 20), E from the temporal plaquette, and the
  * NGP particles of LightConeNGPParticleCreator (round(aL/dt) per cell, 100+100
- * refinement sweeps), which are attached to the handle.  OPX_F64 handles,
- * beam along direction 0.  Call opx_initialize afterwards (Simulation.initialize). */
+ * refinement sweeps), appended to the handle's particle list.  The Gauss
+ * violation that seeds the particles is taken with zero grid charge, as before
+ * Simulation.initialize.  use_seed == 0 draws an unseeded stream.  OPX_F64
+ * handles, beam along direction 0.  Call opx_initialize afterwards. */
 int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
 
 /* ---- seeded synthetic initial conditions (no counterpart in the reference) ---- */

@@ -18,6 +18,7 @@ LIB = os.path.join(LIBDIR, "libopixi_gpu.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas",
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 PER_FILE = {"cpic_kernels.cu": ["--fmad=false"]}
 

@@ -26,12 +26,14 @@
 
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <string>
 #include <vector>
 
 #include <cufft.h>
 
 #include "internal.h"
+#include "java_random.h"
 
 namespace opx {
 
@@ -59,37 +61,6 @@ struct FFTLib {
     }
 };
 static FFTLib g_fft;
-
-// ---------------------------------------------------------------- java.util.Random
-// The generator specified in the Java SE API documentation: a 48-bit linear
-// congruential generator (multiplier 0x5DEECE66D, addend 0xB); nextDouble
-// takes 26 + 27 bits; nextGaussian is the polar method with one cached value.
-struct JavaRandom {
-    uint64_t seed;
-    bool have = false;
-    double next_g = 0;
-    explicit JavaRandom(int64_t s) { seed = ((uint64_t)s ^ 0x5DEECE66DULL) & ((1ULL << 48) - 1); }
-    int next(int bits) {
-        seed = (seed * 0x5DEECE66DULL + 0xBULL) & ((1ULL << 48) - 1);
-        return (int)(int64_t)(seed >> (48 - bits));
-    }
-    double next_double() {
-        return (double)(((int64_t)next(26) << 27) + next(27)) * (1.0 / (double)(1LL << 53));
-    }
-    double next_gaussian() {
-        if (have) { have = false; return next_g; }
-        double v1, v2, s;
-        do {
-            v1 = 2 * next_double() - 1;
-            v2 = 2 * next_double() - 1;
-            s = v1 * v1 + v2 * v2;
-        } while (s >= 1 || s == 0);
-        const double mul = std::sqrt(-2 * std::log(s) / s);
-        next_g = v2 * mul;
-        have = true;
-        return v1 * mul;
-    }
-};
 
 // ---------------------------------------------------------------- kernels
 // V = identity in the direction-0 slot of a link-shaped buffer
@@ -193,7 +164,8 @@ __global__ void k_gauge_links(const double *__restrict__ Vl, double *__restrict_
     site_coords(L, s, x);
     const Nbr nb = neighbours(L, s, x);
     for (int d = 0; d < 3; d++) {
-        if (d == direction) { Cp.store(d, s, G::identity()); continue; }
+        // the copy's longitudinal links are the grid's own (Grid(Grid) copies every cell)
+        if (d == direction) { Cp.store(d, s, Up.load(d, s)); continue; }
         const auto V1 = Vp.load(0, s), V2 = Vp.load(0, nb.fwd[d]);
         Up.store(d, s, G::mul_adj(G::mul(V1, Up.load(d, s)), V2));
         Cp.store(d, s, G::mul_adj(V1, V2));
@@ -444,9 +416,12 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
     const int B = 256;
     if (!rc) {
         // 1. MV charges (host random stream, MVModel.java:114-131)
-        JavaRandom rand(nu.seed);
+        JavaRandom rand((int64_t)nu.seed);
         const double width = nu.mu * c.L.g / std::sqrt(aL * aT * aT);
+        // org.apache.commons.math3.analysis.function.Gaussian(mean, sigma).value:
+        // norm * exp(-d * d * i2s2), norm = 1/(sigma sqrt(2 pi)), i2s2 = 0.5 (1/sigma)^2
         const double norm = 1.0 / (nu.width * std::sqrt(2.0 * 3.141592653589793));
+        const double is = 1.0 / nu.width, i2s2 = 0.5 * is * is;
         std::vector<double> tmp(V);
         const double box = n0 * aL;
         const double zmin = std::max(nu.location - box / 2.0, 0.0), zmax = std::min(nu.location + box / 2.0, box);
@@ -454,9 +429,8 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
         for (int comp = 0; comp < NA && !rc; comp++) {
             for (long s = 0; s < V; s++) {
                 const int z = (int)(s / ntr);
-                const double x = z * aL;
-                const double x1 = (x - nu.location) / nu.width;
-                const double profile = std::sqrt(norm * std::exp(-0.5 * x1 * x1));
+                const double d = z * aL - nu.location;
+                const double profile = std::sqrt(norm * std::exp(-d * d * i2s2));
                 tmp[s] = rand.next_gaussian() * width * profile;
             }
             cudaMemcpyAsync(phi, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice, c.stream);
@@ -573,16 +547,28 @@ extern "C" int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
     for (int q = 0; q < n; q++) {
         if (nuclei[q].direction != 0) { c.err = "opx_cgc_mv: the beam must run along direction 0"; return OPX_ERR_UNSUPPORTED; }
         if (nuclei[q].orientation != 1 && nuclei[q].orientation != -1) { c.err = "opx_cgc_mv: orientation must be +1 or -1"; return OPX_ERR_INVALID; }
-        if (!(nuclei[q].width > 0) || !(nuclei[q].uvt > 0)) { c.err = "opx_cgc_mv: width and UV cutoff must be > 0"; return OPX_ERR_INVALID; }
+        if (!(nuclei[q].width > 0) || !(nuclei[q].uvt >= 0)) { c.err = "opx_cgc_mv: width must be > 0 and the UV cutoff >= 0"; return OPX_ERR_INVALID; }
     }
     if (!g_fft.load(c.err)) return OPX_ERR_UNSUPPORTED;
-    std::vector<double> p0, p1, v, q;
-    std::vector<int32_t> d;
-    for (int k = 0; k < n; k++) {
-        int rc = cgc_nucleus(c, nuclei[k], p0, p1, v, q, d);
+    // particles already on the handle stay first in the list (s.particles.add appends)
+    const long n0 = c.P.n;
+    const int nar = c.na_ref;
+    std::vector<double> p0(3 * n0), p1(3 * n0), v(3 * n0), q0((size_t)nar * n0), q1((size_t)nar * n0);
+    std::vector<int32_t> d(n0);
+    if (n0 > 0) {
+        opx_particles cur{n0, p0.data(), p1.data(), v.data(), q0.data(), q1.data(), d.data(), nullptr};
+        int rc = opx_particles_download(ctx, &cur);
         if (rc) return rc;
     }
-    // Q1 = Q0 for all particles (LightConeNGPParticleCreator.java:231-234)
-    opx_particles P{(long)d.size(), p0.data(), p1.data(), v.data(), q.data(), q.data(), d.data(), nullptr};
+    for (int k = 0; k < n; k++) {
+        opx_mv_nucleus nu = nuclei[k];
+        // MVModel without randomSeed draws from an unseeded java.util.Random
+        if (!nu.use_seed) nu.seed = (int)std::random_device{}();
+        int rc = cgc_nucleus(c, nu, p0, p1, v, q0, d);
+        if (rc) return rc;
+    }
+    // Q1 = Q0 for the new particles (LightConeNGPParticleCreator.java:229-234)
+    q1.insert(q1.end(), q0.begin() + (size_t)nar * n0, q0.end());
+    opx_particles P{(long)d.size(), p0.data(), p1.data(), v.data(), q0.data(), q1.data(), d.data(), nullptr};
     return opx_particles_upload(ctx, &P);
 }

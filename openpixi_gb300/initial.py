@@ -43,7 +43,7 @@ def from_yaml(ics):
                                         o.get("gaussProject", True)))
     if ics.get("CGC") is not None:
         from .cgc import CGCInitialCondition
-        out.append(CGCInitialCondition.from_yaml(ics["CGC"]))
+        out.extend(CGCInitialCondition.from_yaml(ics["CGC"]))
     unsupported = set(ics) - {"randomGaussian", "CGC"}
     if unsupported:
         raise NotImplementedError(f"initial conditions not provided: {sorted(unsupported)}")

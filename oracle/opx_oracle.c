@@ -1052,3 +1052,361 @@ int orc_gauss_restoration(const orc_params *p, double *U, double *Unext, double 
     free(gv); free(bE); free(bUn);
     return i;
 }
+
+/* ------------------------------------------------------------------------- */
+/* CGC initial conditions (physics/initial/CGC)                               */
+/* ------------------------------------------------------------------------- */
+
+/* java.util.Random as the Java SE API documentation specifies it: 48-bit LCG
+ * (multiplier 0x5DEECE66D, addend 0xB), nextDouble from 26 + 27 bits,
+ * nextGaussian by the polar method with one cached deviate. */
+typedef struct { uint64_t seed; int have; double next; } jrand;
+
+/* StrictMath.log: the fdlibm algorithm (e_log.c, the method Java specifies for
+ * StrictMath): x = 2^k (1+f) with sqrt(2)/2 < 1+f < sqrt(2), s = f/(2+f),
+ * log(1+f) = f - s (f - R(s^2)) with a degree-14 even minimax polynomial R,
+ * and k ln2 split into a high and a low part.  Finite x > 0 only. */
+static double strict_log(double x)
+{
+    static const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10,
+                        two54 = 1.80143985094819840000e+16,
+                        Lg1 = 6.666666666666735130e-01, Lg2 = 3.999999999940941908e-01,
+                        Lg3 = 2.857142874366239149e-01, Lg4 = 2.222219843214978396e-01,
+                        Lg5 = 1.818357216161805012e-01, Lg6 = 1.531383769920937332e-01,
+                        Lg7 = 1.479819860511658591e-01;
+    uint64_t bits;
+    memcpy(&bits, &x, 8);
+    int32_t hx = (int32_t)(bits >> 32);
+    uint32_t lx = (uint32_t)bits;
+    int32_t k = 0;
+    if (hx < 0x00100000) { /* subnormal */
+        (void)lx;
+        k -= 54;
+        x *= two54;
+        memcpy(&bits, &x, 8);
+        hx = (int32_t)(bits >> 32);
+    }
+    k += (hx >> 20) - 1023;
+    hx &= 0x000fffff;
+    int32_t i = (hx + 0x95f64) & 0x100000;
+    bits = ((uint64_t)(uint32_t)(hx | (i ^ 0x3ff00000)) << 32) | (bits & 0xffffffffULL);
+    memcpy(&x, &bits, 8);
+    k += (i >> 20);
+    double f = x - 1.0, dk, R;
+    if ((0x000fffff & (2 + hx)) < 3) {
+        if (f == 0.0) {
+            if (k == 0) return 0.0;
+            dk = (double)k;
+            return dk * ln2_hi + dk * ln2_lo;
+        }
+        R = f * f * (0.5 - 0.33333333333333333 * f);
+        if (k == 0) return f - R;
+        dk = (double)k;
+        return dk * ln2_hi - ((R - dk * ln2_lo) - f);
+    }
+    double s = f / (2.0 + f);
+    dk = (double)k;
+    double z = s * s;
+    i = hx - 0x6147a;
+    double w = z * z;
+    int32_t j = 0x6b851 - hx;
+    double t1 = w * (Lg2 + w * (Lg4 + w * Lg6));
+    double t2 = z * (Lg1 + w * (Lg3 + w * (Lg5 + w * Lg7)));
+    i |= j;
+    R = t2 + t1;
+    if (i > 0) {
+        double hfsq = 0.5 * f * f;
+        if (k == 0) return f - (hfsq - s * (hfsq + R));
+        return dk * ln2_hi - ((hfsq - (s * (hfsq + R) + dk * ln2_lo)) - f);
+    }
+    if (k == 0) return f - s * (f - R);
+    return dk * ln2_hi - ((s * (f - R) - dk * ln2_lo) - f);
+}
+
+static void jrand_seed(jrand *r, int64_t s)
+{
+    r->seed = ((uint64_t)s ^ 0x5DEECE66DULL) & ((1ULL << 48) - 1);
+    r->have = 0;
+}
+static int32_t jrand_next(jrand *r, int bits)
+{
+    r->seed = (r->seed * 0x5DEECE66DULL + 0xBULL) & ((1ULL << 48) - 1);
+    return (int32_t)(int64_t)(r->seed >> (48 - bits));
+}
+static double jrand_double(jrand *r)
+{
+    int64_t hi = (int64_t)jrand_next(r, 26), lo = (int64_t)jrand_next(r, 27);
+    return (double)((hi << 27) + lo) * 0x1.0p-53;
+}
+static double jrand_gaussian(jrand *r)
+{
+    if (r->have) { r->have = 0; return r->next; }
+    double v1, v2, s;
+    do {
+        v1 = 2 * jrand_double(r) - 1;
+        v2 = 2 * jrand_double(r) - 1;
+        s = v1 * v1 + v2 * v2;
+    } while (s >= 1 || s == 0);
+    double m = sqrt(-2 * strict_log(s) / s);
+    r->next = v2 * m;
+    r->have = 1;
+    return v1 * m;
+}
+
+double orc_strict_log(double x) { return strict_log(x); }
+
+void orc_java_random(int64_t seed, int kind, long count, double *out)
+{
+    jrand r;
+    jrand_seed(&r, seed);
+    for (long i = 0; i < count; i++) {
+        if (kind == 0) out[i] = jrand_gaussian(&r);
+        else if (kind == 1) out[i] = jrand_double(&r);
+        else out[i] = (double)jrand_next(&r, 32);
+    }
+}
+
+/* MVModel.initialize, random part (physics/initial/CGC/MVModel.java:113-132):
+ * one java.util.Random stream over all components in site order, scaled by
+ * g mu / sqrt(aL aT^2) and the square root of the longitudinal Gaussian profile
+ * (org.apache.commons.math3.analysis.function.Gaussian 3.5: norm * exp(-d*d*i2s2),
+ * norm = 1/(sigma sqrt(2 pi)), i2s2 = 0.5 (1/sigma)^2).  out: [ncomp][V]. */
+void orc_mv_charges(const orc_params *p, int direction, double location, double width, double mu,
+                    int64_t seed, double *out)
+{
+    long V = vol(p);
+    int ncomp = p->nc > 1 ? p->nc * p->nc - 1 : 1;
+    double aL = p->a[direction], aT = p->a[(direction + 1) % 3];
+    double is = 1.0 / width, i2s2 = 0.5 * is * is;
+    double norm = 1.0 / (width * sqrt(2.0 * M_PI));
+    double colorWidth = mu * p->g / sqrt(aL * aT * aT);
+    jrand r;
+    jrand_seed(&r, seed);
+    for (int j = 0; j < ncomp; j++)
+        for (long i = 0; i < V; i++) {
+            int pos[3];
+            cell_pos(p, i, pos);
+            double longPos = pos[direction] * p->a[direction];
+            double d = longPos - location;
+            double profile = sqrt(norm * exp(-d * d * i2s2));
+            out[(size_t)j * V + i] = jrand_gaussian(&r) * colorWidth * profile;
+        }
+}
+
+/* LightConePoissonSolverImproved.solve after the 2D Poisson solves
+ * (physics/initial/CGC/LightConePoissonSolverImproved.java:92-220).
+ * phi: [ncomp][V] generator components (phi0[i].set(c, .)); U, Unext, E are
+ * updated in place (reference layout); gauss: [V][na], the Gauss violation of
+ * the nucleus alone (grid copy with its own links, rho of the grid = 0). */
+void orc_cgc_solve(const orc_params *p, int direction, int orientation, const double *phi,
+                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    int ncomp = nc > 1 ? nc * nc - 1 : 1;
+    long V = vol(p);
+    int nL = p->n[direction];
+    long ntr = V / nL;
+    double aL = p->a[direction];
+    double *Vw = malloc((size_t)V * ng * sizeof(double));
+    double *phiA = malloc((size_t)V * na * sizeof(double));
+    double *Uc = malloc((size_t)V * 3 * ng * sizeof(double));
+    double *Unc = malloc((size_t)V * 3 * ng * sizeof(double));
+    double *Ec = malloc((size_t)V * 3 * na * sizeof(double));
+    double zero[NA_MAX] = {0};
+    for (long i = 0; i < V; i++) {
+        double gen[8];
+        for (int c = 0; c < ncomp; c++) gen[c] = phi[(size_t)c * V + i];
+        orc_gen_to_alg(nc, gen, phiA + (size_t)i * na);
+        group_identity(nc, Vw + (size_t)i * ng);
+    }
+    /* grid copy: every cell copied from the grid (Grid(Grid), Cell.copyFrom) */
+    memcpy(Uc, U, (size_t)V * 3 * ng * sizeof(double));
+    memcpy(Unc, Unext, (size_t)V * 3 * ng * sizeof(double));
+    memcpy(Ec, E, (size_t)V * 3 * na * sizeof(double));
+    /* Wilson lines (:100-124); the transverse index runs over the other two
+     * dimensions in order, so for direction 0 it is the site's offset within the sheet */
+    double gaugeFactor = -p->g * aL;
+    for (int k = 0; k < nL; k++) {
+        int z = orientation < 0 ? k : nL - k - 1;
+        for (long t = 0; t < ntr; t++) {
+            /* transverse cell position -> grid position with the longitudinal slot z */
+            int pos[3], tp[2], dims_t[2], m = 0;
+            for (int d = 0; d < 3; d++) if (d != direction) dims_t[m++] = p->n[d];
+            tp[0] = (int)(t / dims_t[1]);
+            tp[1] = (int)(t % dims_t[1]);
+            m = 0;
+            for (int d = 0; d < 3; d++) pos[d] = d == direction ? z : tp[m++];
+            long index = ((long)pos[0] * p->n[1] + pos[1]) * p->n[2] + pos[2];
+            long indexL = orc_shift(p, index, direction, orientation);
+            double a[NA_MAX], W[NG_MAX], t2[NG_MAX];
+            const double *src = phiA + (size_t)(orientation == -1 ? indexL : index) * na;
+            for (int c = 0; c < na; c++) a[c] = src[c] * gaugeFactor;
+            orc_alg_getlink(nc, a, W);
+            orc_group_mult(nc, Vw + (size_t)indexL * ng, W, t2);
+            memcpy(Vw + (size_t)index * ng, t2, sizeof(double) * ng);
+        }
+    }
+    /* links at t = -dt/2 (:143-157) */
+    for (long i = 0; i < V; i++)
+        for (int d = 0; d < 3; d++) {
+            if (d == direction) continue;
+            long is = orc_shift(p, i, d, 1);
+            double adj[NG_MAX], t1[NG_MAX];
+            orc_group_adj(nc, Vw + (size_t)is * ng, adj);
+            orc_group_mult(nc, Vw + (size_t)i * ng, U + ((size_t)i * 3 + d) * ng, t1);
+            orc_group_mult(nc, t1, adj, U + ((size_t)i * 3 + d) * ng);
+            orc_group_mult(nc, Vw + (size_t)i * ng, adj, Uc + ((size_t)i * 3 + d) * ng);
+        }
+    /* improved V at t = dt/2 (:160-185), M = 20 path-ordered factors */
+    const int M = 20;
+    for (long i = 0; i < V; i++) {
+        double IW[NG_MAX], W[NG_MAX], t1[NG_MAX], ph[NA_MAX];
+        group_identity(nc, IW);
+        long is = orc_shift(p, i, direction, -1);
+        for (int m = 0; m < M; m++) {
+            double z = (m + 0.5) / ((double)2 * M);
+            double FL = orientation == 1 ? +z + 0.5 : -z + 0.5;
+            double FR = orientation == 1 ? -z + 0.5 : +z + 0.5;
+            for (int c = 0; c < na; c++)
+                ph[c] = phiA[(size_t)is * na + c] * FL + phiA[(size_t)i * na + c] * FR;
+            double f = -p->g * p->dt / ((double)M);
+            for (int c = 0; c < na; c++) ph[c] = ph[c] * f;
+            orc_alg_getlink(nc, ph, W);
+            orc_group_mult(nc, IW, W, t1);
+            memcpy(IW, t1, sizeof(double) * ng);
+        }
+        orc_group_mult(nc, Vw + (size_t)i * ng, IW, t1);
+        memcpy(Vw + (size_t)i * ng, t1, sizeof(double) * ng);
+    }
+    /* links at t = dt/2 (:188-202) */
+    for (long i = 0; i < V; i++)
+        for (int d = 0; d < 3; d++) {
+            if (d == direction) continue;
+            long is = orc_shift(p, i, d, 1);
+            double adj[NG_MAX], t1[NG_MAX];
+            orc_group_adj(nc, Vw + (size_t)is * ng, adj);
+            orc_group_mult(nc, Vw + (size_t)i * ng, Unext + ((size_t)i * 3 + d) * ng, t1);
+            orc_group_mult(nc, t1, adj, Unext + ((size_t)i * 3 + d) * ng);
+            orc_group_mult(nc, Vw + (size_t)i * ng, adj, Unc + ((size_t)i * 3 + d) * ng);
+        }
+    /* E at t = 0 from the temporal plaquette (:205-210, Grid.getEFromLinks) */
+    for (long i = 0; i < V; i++)
+        for (int j = 0; j < 3; j++) {
+            double adj[NG_MAX], pl[NG_MAX], v[NA_MAX];
+            orc_group_adj(nc, U + ((size_t)i * 3 + j) * ng, adj);
+            orc_group_mult(nc, Unext + ((size_t)i * 3 + j) * ng, adj, pl);
+            orc_group_proj(nc, pl, v);
+            for (int c = 0; c < na; c++) E[((size_t)i * 3 + j) * na + c] = v[c] * (-1.0 / p->dt);
+            orc_group_adj(nc, Uc + ((size_t)i * 3 + j) * ng, adj);
+            orc_group_mult(nc, Unc + ((size_t)i * 3 + j) * ng, adj, pl);
+            orc_group_proj(nc, pl, v);
+            for (int c = 0; c < na; c++) Ec[((size_t)i * 3 + j) * na + c] = v[c] * (-1.0 / p->dt);
+        }
+    /* Gauss violation of the copy (:213-220) */
+    double *rho0 = calloc((size_t)V * na, sizeof(double));
+    for (long i = 0; i < V; i++) {
+        if (!active || active[i]) orc_gauss_constraint(p, Uc, Ec, rho0, i, gauss + (size_t)i * na);
+        else memcpy(gauss + (size_t)i * na, zero, sizeof(double) * na);
+    }
+    free(rho0); free(Vw); free(phiA); free(Uc); free(Unc); free(Ec);
+}
+
+static long ring(long i, long n) { return (i % n + n) % n; }
+
+/* LightConeNGPParticleCreator.initializeParticles (physics/initial/CGC/
+ * LightConeNGPParticleCreator.java:110-235) for beam direction 0.
+ * Returns the number of particles; the arrays are filled when cap >= that
+ * number: pos0, pos1, vel [np][3], Q [np][na] (Q0 = Q1). */
+long orc_cgc_particles(const orc_params *p, const double *gauss, int orientation, long cap,
+                       double *pos0, double *pos1, double *vel, double *Q)
+{
+    int nc = p->nc, na = orc_na(nc);
+    const int direction = 0;
+    long V = vol(p);
+    int lnum = p->n[0];
+    long ntr = V / lnum;
+    int ppc = (int)lround(p->a[direction] / p->dt);
+    if (ppc < 1) return -1;
+    double *maxCharges = malloc(sizeof(double) * lnum), globalMax = 0.0;
+    for (int z = 0; z < lnum; z++) {
+        double mx = 0.0;
+        for (long j = 0; j < ntr; j++) {
+            double charge = sqrt(orc_alg_square(nc, gauss + (size_t)(z * ntr + j) * na));
+            if (mx < charge) mx = charge;
+        }
+        maxCharges[z] = mx;
+        if (globalMax < mx) globalMax = mx;
+    }
+    double cutoff = globalMax * 10E-10;
+    int zStart = 0, zEnd = lnum - 1;
+    for (int z = 0; z < lnum; z++) if (maxCharges[z] > cutoff) { zStart = z; break; }
+    for (int z = zEnd - 1; z >= 0; z--) if (maxCharges[z] > cutoff) { zEnd = z; break; }
+    free(maxCharges);
+    long np = (long)(zEnd - zStart + 1) * ntr * ppc;
+    if (cap < np) return np;
+    long k = 0;
+    for (int z = zStart; z <= zEnd; z++)
+        for (long i = 0; i < ntr; i++) {
+            int gp[3] = {z, (int)(i / p->n[2]), (int)(i % p->n[2])};
+            for (int j = 0; j < ppc; j++, k++) {
+                double x = (1.0 * j - ppc / 2) / (ppc);
+                double dz = x * p->a[direction];
+                for (int d = 0; d < 3; d++) {
+                    double fix = 10E-12 * p->a[d];
+                    pos0[k * 3 + d] = gp[d] * p->a[d] + fix;
+                    pos1[k * 3 + d] = gp[d] * p->a[d] + fix;
+                    if (d == direction) {
+                        pos0[k * 3 + d] += 0.0 * orientation + dz;
+                        pos1[k * 3 + d] += (0.0 + p->dt) * orientation + dz;
+                    }
+                    vel[k * 3 + d] = d == direction ? 1.0 * orientation : 0.0;
+                }
+                int32_t c[3];
+                orc_ngp(p, pos0 + k * 3, c);
+                const double *gsrc = gauss + (size_t)cell_index(p, c) * na;
+                for (int a = 0; a < na; a++) Q[k * na + a] = gsrc[a] * (1.0 / ppc);
+            }
+        }
+    /* charge refinement per transverse column (:211-227, refine2 :237-262,
+     * refine4 :265-296); the column's list runs over z, then over j */
+    long n = (long)(zEnd - zStart + 1) * ppc;
+    for (long t = 0; t < ntr; t++) {
+#define PIDX(ii) ((((ring((ii), n)) / ppc) * ntr + t) * ppc + (ring((ii), n)) % ppc)
+        for (int it = 0; it < 100; it++)
+            for (long i = 0; i < n; i++) {
+                long jm = i % ppc;
+                if (!(jm >= 0 && jm < ppc - 1)) continue;
+                double *Q0 = Q + PIDX(i - 1) * na, *Q1 = Q + PIDX(i) * na, *Q2 = Q + PIDX(i + 1) * na,
+                       *Q3 = Q + PIDX(i + 2) * na;
+                for (int a = 0; a < na; a++) {
+                    double DQ = Q0[a] * -1;
+                    DQ = DQ + Q1[a] * 3;
+                    DQ = DQ + Q2[a] * -3;
+                    DQ = DQ + Q3[a] * 1;
+                    DQ = DQ * (1.0 / 4.0);
+                    Q1[a] = Q1[a] + DQ * -1.0;
+                    Q2[a] = Q2[a] + DQ * 1.0;
+                }
+            }
+        for (int it = 0; it < 100; it++)
+            for (long i = 0; i < n; i++) {
+                long jm = i % ppc;
+                if (!(jm >= 0 && jm < ppc - 1)) continue;
+                double *Q0 = Q + PIDX(i - 2) * na, *Q1 = Q + PIDX(i - 1) * na, *Q2 = Q + PIDX(i) * na,
+                       *Q3 = Q + PIDX(i + 1) * na, *Q4 = Q + PIDX(i + 2) * na, *Q5 = Q + PIDX(i + 3) * na;
+                for (int a = 0; a < na; a++) {
+                    double DQ = Q0[a] * 1;
+                    DQ = DQ + Q1[a] * -5;
+                    DQ = DQ + Q2[a] * 10;
+                    DQ = DQ + Q3[a] * -10;
+                    DQ = DQ + Q4[a] * 5;
+                    DQ = DQ + Q5[a] * -1;
+                    DQ = DQ * (1.0 / 12.0);
+                    Q2[a] = Q2[a] + DQ * -1.0;
+                    Q3[a] = Q3[a] + DQ * 1.0;
+                }
+            }
+#undef PIDX
+    }
+    return np;
+}

@@ -136,6 +136,21 @@ int orc_gauss_restoration(const orc_params *p, double *U, double *Unext, double 
                           const double *rho, double gamma, int maxit, double absval,
                           double *final_violation);
 
+/* ---- CGC initial conditions (physics/initial/CGC) ---- */
+/* java.util.Random(seed): kind 0 nextGaussian, 1 nextDouble, 2 nextInt */
+void orc_java_random(int64_t seed, int kind, long count, double *out);
+/* StrictMath.log (fdlibm) */
+double orc_strict_log(double x);
+/* MVModel.initialize before regulation: out [ncomp][V] generator components */
+void orc_mv_charges(const orc_params *p, int direction, double location, double width, double mu,
+                    int64_t seed, double *out);
+/* LightConePoissonSolverImproved.solve after the Poisson solves */
+void orc_cgc_solve(const orc_params *p, int direction, int orientation, const double *phi,
+                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss);
+/* LightConeNGPParticleCreator.initializeParticles (beam direction 0) */
+long orc_cgc_particles(const orc_params *p, const double *gauss, int orientation, long cap,
+                       double *pos0, double *pos1, double *vel, double *Q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,92 @@
+"""CPU checks of the CGC oracle (MV model, light-cone Poisson solver, particle creator).
+
+The reference ships no test for these classes, so the oracle is pinned by
+published values of java.util.Random (the generator the MV charges come
+from) and by the properties the reference's construction guarantees:
+the 2D Poisson equation holds sheet by sheet, refinement moves charge only
+within a cell, and the particles' charge cancels the Gauss violation of the
+fields after Simulation.initialize.
+"""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def cgc(orc):
+    from oracle import cgc as m
+    return m
+
+
+def test_java_random_known_values(cgc):
+    # values printed by java.util.Random as documented in the Java SE API
+    assert cgc.java_random(42, 2, 1)[0] == -1170105035.0
+    assert cgc.java_random(42, 1, 1)[0] == 0.7275636800328681
+    assert cgc.java_random(42, 0, 1)[0] == 1.1419053154730547
+    assert cgc.java_random(0, 0, 1)[0] == 0.8025330637390305
+    # nextGaussian draws pairs: the second of a pair comes from the cache
+    g = cgc.java_random(7, 0, 6)
+    assert len(set(g.tolist())) == 6
+
+
+def test_poisson2d_solves_lattice_laplacian(cgc):
+    rng = np.random.default_rng(1)
+    dims = (4, 8, 6)
+    rho = rng.normal(size=int(np.prod(dims)))
+    phi = cgc.poisson2d(rho, dims, aT=0.7).reshape(dims)
+    lap = sum(np.roll(phi, 1, ax) + np.roll(phi, -1, ax) - 2 * phi for ax in (1, 2)) / 0.7 ** 2
+    r = rho.reshape(dims)
+    r = r - r.mean(axis=(1, 2), keepdims=True)
+    assert np.abs(-lap - r).max() < 1e-13
+
+
+def test_regulation_removes_kt_zero_modes(cgc):
+    rng = np.random.default_rng(2)
+    dims = (8, 8, 8)
+    r = cgc.regulate(rng.normal(size=512), dims, uvt=4.44, long_width=0.0, ir=0.0, aT=1.0, aL=1.0).reshape(dims)
+    # every kT = 0 mode is cut, so each longitudinal sheet sums to zero
+    assert np.abs(r.sum(axis=(1, 2))).max() < 1e-12
+    # with no UV cut, no IR mass and no longitudinal smoothing only the kT = 0 modes go
+    x = rng.normal(size=512).reshape(dims)
+    y = cgc.regulate(x.reshape(-1), dims, uvt=10.0, long_width=0.0, ir=0.0, aT=1.0, aL=1.0).reshape(dims)
+    assert np.allclose(y, x - x.mean(axis=(1, 2), keepdims=True), atol=1e-13)
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_single_nucleus_gauss_law_after_initialize(orc, cgc, nc):
+    g = orc.OracleGrid(nc, (32, 6, 6), dt=0.5)
+    P, info = cgc.cgc_mv(g, [cgc.MVNucleus(orientation=1, location=16.0, width=1.5, mu=0.5, seed=11)])
+    ppc = 2
+    assert P.n % (36 * ppc) == 0
+    # cell sums of the refined charges equal the Gauss violation (refinement is cell-local)
+    gauss = info[0]["gauss"]
+    rho = np.zeros_like(gauss)
+    cells = np.rint(P.pos0[:, 0]).astype(int) * 36 + np.rint(P.pos0[:, 1]).astype(int) * 6 + np.rint(P.pos0[:, 2]).astype(int)
+    np.add.at(rho, cells, P.Q0)
+    z = np.arange(g.V) // 36
+    zs = np.unique(np.rint(P.pos0[:, 0]).astype(int))
+    inside = np.isin(z, zs)
+    assert np.abs(rho[inside] - gauss[inside]).max() < 1e-12 * np.abs(gauss).max()
+    sim = orc.OracleSimulation(g, P)
+    sim.initialize()
+    gmax = np.abs(g.rho).max()
+    assert np.abs(g.gauss_field()).max() < 1e-8 * gmax
+    for _ in range(10):
+        sim.step()
+    assert np.abs(g.gauss_field()).max() < 1e-8 * gmax
+
+
+def test_particle_layout(orc, cgc):
+    g = orc.OracleGrid(2, (24, 4, 4), dt=0.25)
+    P, _ = cgc.cgc_mv(g, [cgc.MVNucleus(orientation=-1, location=12.0, width=1.0, mu=0.5, seed=3)])
+    ppc = 4
+    nz = P.n // (16 * ppc)
+    assert P.n == nz * 16 * ppc
+    # particle k = ((z - zStart) * ntr + t) * ppc + j
+    k = np.arange(P.n)
+    j = k % ppc
+    t = (k // ppc) % 16
+    z0 = int(np.rint(P.pos0[0, 0] + 0.5 * 1.0))
+    assert np.allclose(P.pos0[:, 0], (z0 + k // (ppc * 16)) + (j - ppc // 2) / ppc + 1e-11, atol=1e-12)
+    assert np.array_equal(P.pos0[:, 1], np.floor(P.pos0[:, 1]) + 1e-11) or np.allclose(P.pos0[:, 1], t // 4 + 1e-11)
+    assert np.allclose(P.pos1[:, 0] - P.pos0[:, 0], -0.25)
+    assert np.all(P.vel[:, 0] == -1.0) and np.all(P.vel[:, 1:] == 0.0)
