@@ -10,8 +10,14 @@ updates).  ``value`` is timed with CUDA events on the handle's own stream over
 K steps with the fields resident in HBM (inputs are larger than L2: the links
 alone are 453 MB).  ``e2e`` is the same metric through the public C ABI with
 host buffers: upload of the initial U and E from pinned memory, the K steps
-with the BulkQuantities reductions every 10 steps read back to the host, and
-the download of the final U and E, all inside the timed region.
+each followed by the BulkQuantities reduction read back to the host, and the
+download of the final U and E, all inside the timed region;
+``e2e.per_call_copy`` is FieldSolver.step as a per-call drop-in whose host grid
+stays authoritative (U and E copied in, E and Unext copied out on every call).
+
+Beside the headline line: the batching form (256 SU(2) events in one
+persistent launch) and the CPIC collision form (SU(2) FP64, 256 x 64^2, two MV
+nuclei, 300 steps with per-step diagnostics, oracle check of the first steps).
 
 ``--impl reference`` times the CPU implementation of the path: the reference
 (Java) cannot be built or run on this machine, so its FP64 restatement (the
@@ -291,6 +297,101 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
             "gpu_launches": launches, "max_gauss": max(o.gauss for o in obs)}
 
 
+CGC_DIMS = (256, 64, 64)
+
+
+def cgc_nuclei():
+    """Two MV nuclei of the CPIC collision workload (YamlMVModel defaults for the
+    UV cutoff 4.44, coherence length 0 and IR coefficient 0)."""
+    base = {"direction": 0, "width": 4.0, "mu": 0.5, "use_seed": 1, "uvt": 4.44, "coherence": 0.0, "ir": 0.0}
+    return [dict(base, orientation=1, location=64.0, seed=1), dict(base, orientation=-1, location=192.0, seed=2)]
+
+
+def bench_cgc(device, nsteps=300, oracle_steps=2):
+    """CPIC collision form: SU(2) FP64, lattice 256 x 64^2 (beam along dimension 0),
+    a = 1, dt = 0.5, g = 1, two MV nuclei (mu = 0.5, width 4, seeds 1 and 2) with
+    round(a/dt) = 2 NGP particles per cell; 300 steps of Simulation.step with the
+    ProjectedEnergyDensity (4 x 256) and BulkQuantities diagnostics every step.
+    The oracle repeats the initial condition and the first steps at full size on
+    the host for a parity check."""
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    h = opx.Handle(2, CGC_DIMS, a=1.0, dt=0.5, g=1.0, precision=N.OPX_F64, device=device)
+    h.synchronize()
+    t = time.perf_counter()
+    h.cgc_mv(cgc_nuclei())
+    h.synchronize()
+    ic_ms = 1000.0 * (time.perf_counter() - t)
+    np_ = h.np
+    h.initialize()
+    U0, E0 = h.download(N.FIELD_U), h.download(N.FIELD_E)
+    P0 = h.particles_download()
+    h.set_profiling(True)
+    obs0 = h.reduce()
+    e0 = obs0.e2_total + obs0.b2_total
+    gmax = obs0.gauss
+    proj = []
+    h.synchronize()
+    t = time.perf_counter()
+    for _ in range(nsteps):
+        h.step(1)
+        o = h.reduce()
+        proj.append(h.projected_energy(0))
+        gmax = max(gmax, o.gauss)
+    h.synchronize()
+    wall_ms = 1000.0 * (time.perf_counter() - t)
+    ms, counts = h.phase_times()
+    h.set_profiling(False)
+    obs = h.reduce()
+    e1 = obs.e2_total + obs.b2_total
+    links = 3 * int(np.prod(CGC_DIMS))
+    step_ms = (ms[N.PHASE_EOM] + ms[N.PHASE_CPIC]) / nsteps
+    peak, _ = hbm_peak()
+    lu = links / (step_ms / 1000.0)
+    out = {"workload": "SU(2) CPIC collision, 256x64^2, dt=0.5, 2 MV nuclei, FP64", "particles": np_,
+           "steps": nsteps, "ic_ms": ic_ms, "wall_ms_with_diagnostics": wall_ms,
+           "ms_per_step_device": step_ms, "eom_ms_per_step": ms[N.PHASE_EOM] / nsteps,
+           "cpic_ms_per_step": ms[N.PHASE_CPIC] / nsteps, "diagnostics_ms_per_step": ms[N.PHASE_DIA] / nsteps,
+           "link_updates_per_s": lu, "particle_updates_per_s": np_ / (ms[N.PHASE_CPIC] / nsteps / 1000.0),
+           "roofline_frac_eom": 136.0 * links / (ms[N.PHASE_EOM] / nsteps / 1000.0) / 1e9 / peak,
+           "bytes_per_link": 136, "max_gauss_mean_sq": gmax, "energy_start": e0, "energy_end": e1,
+           "projected_energy_rows": [4, CGC_DIMS[0]], "final_T_el_sum": float(proj[-1][0].sum())}
+    # oracle at full size: the initial condition and the first steps
+    try:
+        import oracle
+        from oracle import cgc as ocgc
+        from oracle import OracleSimulation
+        g = oracle.OracleGrid(2, CGC_DIMS, dt=0.5)
+        nus = [ocgc.MVNucleus(orientation=n["orientation"], location=n["location"], width=n["width"], mu=n["mu"],
+                              seed=n["seed"]) for n in cgc_nuclei()]
+        t = time.perf_counter()
+        P, _ = ocgc.cgc_mv(g, nus)
+        ic_cpu = time.perf_counter() - t
+        sim = OracleSimulation(g, P)
+        sim.initialize()
+        h2 = opx.Handle(2, CGC_DIMS, a=1.0, dt=0.5, g=1.0, precision=N.OPX_F64, device=device)
+        h2.upload(N.FIELD_U, U0)
+        h2.upload(N.FIELD_E, E0)
+        h2.particles_upload(P0["pos0"], P0["pos1"], P0["vel"], P0["Q0"], P0["Q1"], P0["dir"])
+        h2.initialize()
+        ic_err = float(np.max(np.abs(U0 - g.U)))
+        t = time.perf_counter()
+        for _ in range(oracle_steps):
+            sim.step()
+        step_cpu = (time.perf_counter() - t) / oracle_steps
+        h2.step(oracle_steps)
+        du = float(np.max(np.abs(h2.download(N.FIELD_U) - g.U)))
+        de = float(np.max(np.abs(h2.download(N.FIELD_E) - g.E)) / max(np.abs(g.E).max(), 1e-300))
+        h2.close()
+        out.update({"oracle_particles": int(P.n), "oracle_ic_s": ic_cpu, "oracle_ms_per_step_1thread": 1000 * step_cpu,
+                    "oracle_ic_max_abs_dU": ic_err, "oracle_steps": oracle_steps,
+                    "oracle_max_abs_dU_after": du, "oracle_max_rel_dE_after": de})
+    except Exception as e:  # the measurement stands without the check
+        out["oracle_check"] = f"skipped: {e}"
+    h.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -301,6 +402,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-cgc", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -380,31 +482,54 @@ def main():
     if not args.no_e2e:
         h2 = make_handle(w, w["prec"], device)
         he = (h2.ng + h2.na_ref) * 8 * links
+        obs_bytes = 13 * 8
         dist.barrier()
         t = time.perf_counter()
         h2.upload(N.FIELD_U, U_host.array)
         h2.upload(N.FIELD_E, E_host.array)
         h2.initialize()
-        nred = 0
         for k in range(args.steps):
             h2.step(1)
-            if (k + 1) % 10 == 0:
-                h2.reduce()
-                nred += 1
+            h2.reduce()
         h2.download(N.FIELD_U, out=U_host.array)
         h2.download(N.FIELD_E, out=E_host.array)
         el = time.perf_counter() - t
         el = dist.max(el)
         e2e = {"value": world * links * args.steps / el, "unit": METRIC,
                "h2d_bytes_per_step": he / args.steps,
-               "d2h_bytes_per_step": (he + nred * 64) / args.steps,
-               "note": "initial U,E uploaded from pinned host memory and final U,E downloaded inside the "
-                       "timed region (bytes amortised over the steps); BulkQuantities read back every 10 steps"}
+               "d2h_bytes_per_step": obs_bytes + he / args.steps,
+               "note": "Simulation.step through the C ABI with the BulkQuantities observables (13 FP64 "
+                       "values) read back to the host after every step; initial U,E uploaded from pinned "
+                       "host memory and final U,E downloaded inside the timed region"}
+        # FieldSolver.step as a per-call drop-in with the host grid authoritative:
+        # every call uploads U and E and downloads E and Unext (reference layout, FP64 host arrays)
+        ncall = max(3, min(args.steps, 20))
+        Un_host = opx.PinnedArray((V, 3, h2.ng))
+        h2.upload(N.FIELD_U, U_host.array)
+        h2.upload(N.FIELD_E, E_host.array)
+        h2.synchronize()
+        dist.barrier()
+        t = time.perf_counter()
+        for k in range(ncall):
+            h2.upload(N.FIELD_U, U_host.array if k == 0 else Un_host.array)
+            h2.upload(N.FIELD_E, E_host.array)
+            h2.update_grid()
+            h2.download(N.FIELD_E, out=E_host.array)
+            h2.download(N.FIELD_UNEXT, out=Un_host.array)
+        el = dist.max(time.perf_counter() - t)
+        e2e["per_call_copy"] = {"value": world * links * ncall / el, "unit": METRIC, "calls": ncall,
+                                "h2d_bytes_per_step": he, "d2h_bytes_per_step": he,
+                                "note": "each FieldSolver.step call copies the whole grid state in and out"}
+        Un_host.free()
         h2.close()
 
     batched = None
     if not args.no_batch and args.workload == "su3_fp32_128":
         batched = bench_batch(device)
+
+    cgc = None
+    if not args.no_cgc and args.workload == "su3_fp32_128":
+        cgc = bench_cgc(device)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -416,6 +541,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": w["prec"], "data": "synthetic",
                 "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64, "batched": batched,
+                "cgc_collision": cgc,
                 "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
                 "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
         print(json.dumps(line), flush=True)
