@@ -462,6 +462,14 @@ def main():
                 "algorithmic_bytes_per_link": w["bpl"], "links_per_launch": links,
                 "kernel": "k_update_grid", "launch_ms": t_launch * 1000.0}
 
+    # ---- the BulkQuantities reduction (one pass: E^2, B^2 from U and Unext, Gauss, rho^2)
+    h.set_profiling(True)
+    for _ in range(10):
+        h.reduce()
+    rms, rn = h.phase_times()
+    h.set_profiling(False)
+    reduce_ms = rms[N.PHASE_DIA] / max(rn[N.PHASE_DIA], 1)
+
     # ---- the plain FP64 GPU path on the same lattice (same initial fields)
     fp64 = None
     if w["prec"] == "f32":
@@ -542,7 +550,7 @@ def main():
                 "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64, "batched": batched,
                 "cgc_collision": cgc,
-                "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
+                "reduce_ms": reduce_ms, "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
                 "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
         print(json.dumps(line), flush=True)
     dist.close()

@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <cstdlib>
+
 #include "internal.h"
 
 using namespace opx;
@@ -107,6 +109,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     c.na = c.nc == 3 ? 8 : 3;
     c.na_ref = c.nc == 3 ? 9 : 3;
     c.prec = cfg->precision;
+    c.pair_kernel = std::getenv("OPX_SU3_SCALAR") == nullptr;
     c.rsize = c.prec == OPX_F64 ? 8 : 4;
     bool ok = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) == cudaSuccess;
     auto al = [&](void **p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) { ok = false; *p = nullptr; } };
@@ -117,8 +120,9 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     // J and rho are FP64 when particles can be attached (FP64 handles), storage precision otherwise
     al(&c.J, nE * c.rsize);
     al(&c.rho, (size_t)V * c.na * c.rsize);
-    c.red_blocks = (int)std::min<long>(grid_for(V, 256), 4L * 152);
-    al((void **)&c.red_part, sizeof(double) * 2 * 8 * c.red_blocks);
+    c.red_blocks = reduction_blocks(V);
+    // 16 doubles per block: the bulk partials, or 2 (slice, split) partials of the projected energy
+    al((void **)&c.red_part, sizeof(double) * 2 * 8 * std::max(c.red_blocks, 2 * c.L.n[0] + 2 * c.L.n[1] + 2 * c.L.n[2]));
     al((void **)&c.red_out, sizeof(double) * 16);
     al((void **)&c.status, sizeof(unsigned));
     if (ok && cudaMallocHost((void **)&c.red_host, sizeof(double) * 16) != cudaSuccess) ok = false;

@@ -57,6 +57,8 @@ template <> struct LatR<Dual> {
     __device__ __forceinline__ static Dual inva2(const Lat &L, int d) { return Dual(LatR<double>::inva2(L, d)); }
     __device__ __forceinline__ static Dual jfac(const Lat &L, int d) { return Dual(LatR<double>::jfac(L, d)); }
     __device__ __forceinline__ static Dual dt(const Lat &L) { return Dual(L.dt); }
+    __device__ __forceinline__ static Dual bfac(const Lat &L, int d) { return Dual(LatR<double>::bfac(L, d)); }
+    __device__ __forceinline__ static Dual gfac(const Lat &L, int d) { return Dual(LatR<double>::gfac(L, d)); }
 };
 
 }  // namespace opx

@@ -15,6 +15,7 @@
 // 0 are resident in L2 while a block works on its plane).
 #include "internal.h"
 #include "leapfrog.cuh"
+#include "su3_pair.cuh"
 
 namespace opx {
 
@@ -31,6 +32,26 @@ k_update_grid(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ 
     if (s >= L.V) return;
     if (active && !active[s]) return;  // Cell.isActive gate (FastTYMSolver.java:51)
     update_site<NC, R, HAS_J, REUNIT>(U, E, J, Unext, L, s);
+}
+
+// SU(3) FP32: two sites per thread in paired FP32 instructions.  Warp w
+// covers sites [64 w, 64 w + 64): lane l takes site 64 w + l and the site 32
+// further, so both halves of a warp read whole warp-sized link blocks.
+// I = int when every link offset fits in 32 bits.
+template <typename I, bool HAS_J, bool REUNIT>
+__global__ void __launch_bounds__(128, 3)
+k_update_grid_su3f_pair(const float *__restrict__ U, float *__restrict__ E, const float *__restrict__ J,
+                        float *__restrict__ Unext, const uint8_t *__restrict__ active, Lat L) {
+    const I t = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+    const I sa = ((t >> 5) << 6) + (t & 31);
+    if (sa >= (I)L.V) return;
+    I sb = sa + 32;
+    bool vb = sb < (I)L.V;
+    if (!vb) sb = sa;
+    const bool va = !active || active[sa];
+    vb = vb && (!active || active[sb]);
+    if (!va && !vb) return;  // Cell.isActive gate (FastTYMSolver.java:51)
+    update_site_pair<I, HAS_J, REUNIT>(U, E, J, Unext, L, sa, sb, va, vb);
 }
 
 template <int NC, typename R>
@@ -56,8 +77,35 @@ __global__ void k_reunit(R *__restrict__ U, Lat L) {
     }
 }
 
+template <typename I>
+static void update_grid_su3f_pair_i(Ctx &c, bool reunit) {
+    const int B = 128;
+    const long threads = ((c.L.V + 63) / 64) * 32;
+    dim3 grid(grid_for(threads, B));
+    const float *U = (const float *)c.U, *J = (const float *)c.J;
+    float *E = (float *)c.E, *Un = (float *)c.Unext;
+    if (c.j_nonzero) {
+        if (reunit) k_update_grid_su3f_pair<I, true, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+        else k_update_grid_su3f_pair<I, true, false><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+    } else {
+        if (reunit) k_update_grid_su3f_pair<I, false, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+        else k_update_grid_su3f_pair<I, false, false><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+    }
+    c.launches++;
+}
+
+static void update_grid_su3f_pair(Ctx &c, bool reunit) {
+    // 32-bit offsets while the largest link offset (3 blocks x 576 floats) fits
+    if (link_elems(c.L.V, 18) < (1L << 31) - 64) update_grid_su3f_pair_i<int>(c, reunit);
+    else update_grid_su3f_pair_i<long>(c, reunit);
+}
+
 template <int NC, typename R>
 static void update_grid_t(Ctx &c, bool reunit) {
+    if (NC == 3 && sizeof(R) == 4 && c.pair_kernel) {
+        update_grid_su3f_pair(c, reunit);
+        return;
+    }
     const int B = 128;
     dim3 grid(grid_for(c.L.V, B));
     const R *U = (const R *)c.U;

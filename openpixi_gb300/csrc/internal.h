@@ -42,6 +42,9 @@ struct Ctx {
     void *U = nullptr, *Unext = nullptr, *E = nullptr, *J = nullptr, *rho = nullptr;
     uint8_t *active = nullptr, *eval = nullptr;  // null = all true
     bool j_nonzero = false;
+    // SU(3) FP32 leapfrog with two sites per thread in paired FP32 instructions
+    // (environment OPX_SU3_SCALAR=1 selects the one-site-per-thread form)
+    bool pair_kernel = true;
     double *staging = nullptr;
     size_t staging_len = 0;  // doubles
     double *red_part = nullptr;
@@ -66,6 +69,7 @@ void launch_update_links(Ctx &c);
 void launch_reunit(Ctx &c, void *links);
 // ---- reductions (reduce_kernels.cu) ----
 void launch_bulk(Ctx &c);  // result in c.red_out[0..7]
+int reduction_blocks(long V);
 void launch_energy_density(Ctx &c, double *dev_out);
 void launch_projected_energy(Ctx &c, int dir, double *dev_out);
 void launch_gauss_field(Ctx &c, double *dev_out);

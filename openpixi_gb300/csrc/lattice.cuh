@@ -29,6 +29,9 @@ struct Lat {
     // precisions, so that FP32 kernels do no FP64 arithmetic or conversions
     double inva2[3], jfac[3];
     float inva2f[3], jfacf[3], dtf;
+    // Grid.getB area factor a_d / (a_j a_k) and Gauss-law factor 1 / (a_i g a_i)
+    double bfac[3], gfac[3];
+    float bfacf[3], gfacf[3];
 };
 
 __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double g) {
@@ -47,6 +50,13 @@ __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double
         L.jfacf[i] = (float)L.jfac[i];
     }
     L.dtf = (float)dt;
+    for (int d = 0; d < 3; d++) {
+        const int j = (d + 1) % 3, k = (d + 2) % 3;
+        L.bfac[d] = a[d] / (a[j] * a[k]);
+        L.gfac[d] = 1.0 / (a[d] * (g * a[d]));
+        L.bfacf[d] = (float)L.bfac[d];
+        L.gfacf[d] = (float)L.gfac[d];
+    }
     return L;
 }
 
@@ -59,6 +69,12 @@ template <> struct LatR<double> {
         return d == 0 ? L.jfac[0] : (d == 1 ? L.jfac[1] : L.jfac[2]);
     }
     __device__ __forceinline__ static double dt(const Lat &L) { return L.dt; }
+    __device__ __forceinline__ static double bfac(const Lat &L, int d) {
+        return d == 0 ? L.bfac[0] : (d == 1 ? L.bfac[1] : L.bfac[2]);
+    }
+    __device__ __forceinline__ static double gfac(const Lat &L, int d) {
+        return d == 0 ? L.gfac[0] : (d == 1 ? L.gfac[1] : L.gfac[2]);
+    }
 };
 template <> struct LatR<float> {
     __device__ __forceinline__ static float inva2(const Lat &L, int d) {
@@ -68,6 +84,12 @@ template <> struct LatR<float> {
         return d == 0 ? L.jfacf[0] : (d == 1 ? L.jfacf[1] : L.jfacf[2]);
     }
     __device__ __forceinline__ static float dt(const Lat &L) { return L.dtf; }
+    __device__ __forceinline__ static float bfac(const Lat &L, int d) {
+        return d == 0 ? L.bfacf[0] : (d == 1 ? L.bfacf[1] : L.bfacf[2]);
+    }
+    __device__ __forceinline__ static float gfac(const Lat &L, int d) {
+        return d == 0 ? L.gfacf[0] : (d == 1 ? L.gfacf[1] : L.gfacf[2]);
+    }
 };
 
 // Periodic neighbour offsets of site s (Grid.shift, Grid.java:802-823).

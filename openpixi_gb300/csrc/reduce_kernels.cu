@@ -10,17 +10,25 @@
 //   k_energy_density   : EnergyDensity.ComponentComputation (EnergyDensity.java:119-166)
 //   k_projected_energy : ProjectedEnergyDensity.EnergyDensityComputation (:114-179)
 //   k_gauss_field      : Grid.getGaussConstraint (Grid.java:944-968) at every cell
+#include <algorithm>
+
 #include "internal.h"
 #include "ksum.cuh"
 #include "observables.cuh"
 
 namespace opx {
 
+// Register caps for 128-thread reduction blocks: 4 blocks per SM (128
+// registers), SU(3) FP64 2 (255).
+template <int NC, typename R> struct RedBounds { static constexpr int minb = 4; };
+template <> struct RedBounds<3, float> { static constexpr int minb = 4; };
+template <> struct RedBounds<3, double> { static constexpr int minb = 2; };
+constexpr int RED_THREADS = 128;
+
 template <int NC, typename R>
-__global__ void __launch_bounds__(256) k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext,
-                                                      const R *__restrict__ E, const R *__restrict__ rho,
-                                                      const uint8_t *__restrict__ eval, Lat L,
-                                                      double *__restrict__ part) {
+__global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
+    k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
+                   const R *__restrict__ rho, const uint8_t *__restrict__ eval, Lat L, double *__restrict__ part) {
     KSum acc[NQ];
     bulk_accumulate<NC, R>(U, Unext, E, rho, eval, L, acc, (long)blockIdx.x * blockDim.x + threadIdx.x,
                            (long)gridDim.x * blockDim.x);
@@ -34,20 +42,27 @@ __global__ void __launch_bounds__(256) k_bulk_partial(const R *__restrict__ U, c
 }
 
 __global__ void k_bulk_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
-    // one thread per quantity, blocks summed in index order
-    const int q = threadIdx.x;
+    // one warp per quantity: lanes take strided blocks, then a fixed-order shuffle tree
+    const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (q >= NQ) return;
     KSum v{0.0, 0.0};
-    for (int b = 0; b < nblocks; b++) ksum_merge(v, KSum{part[((long)b * NQ + q) * 2], part[((long)b * NQ + q) * 2 + 1]});
-    out[q] = v.s + v.c;
+    for (int b = lane; b < nblocks; b += 32)
+        ksum_merge(v, KSum{part[((long)b * NQ + q) * 2], part[((long)b * NQ + q) * 2 + 1]});
+    for (int o = 16; o > 0; o >>= 1) {
+        KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
+        ksum_merge(v, w);
+    }
+    if (lane == 0) out[q] = v.s + v.c;
 }
+
+int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
 
 template <int NC, typename R>
 static void bulk_t(Ctx &c) {
-    const int B = 256;
-    k_bulk_partial<NC, R><<<c.red_blocks, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
-                                                            (const R *)c.rho, c.eval, c.L, c.red_part);
-    k_bulk_final<<<1, 32, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
+    k_bulk_partial<NC, R><<<c.red_blocks, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
+                                                                     (const R *)c.E, (const R *)c.rho, c.eval, c.L,
+                                                                     c.red_part);
+    k_bulk_final<<<1, 32 * NQ, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
     c.launches += 2;
 }
 
@@ -89,23 +104,23 @@ __global__ void k_energy_density(const R *__restrict__ U, const R *__restrict__ 
     out[s] = en;
 }
 
-// One block per slice x_dir = k; four sums T_el, T_mag, L_el, L_mag.
+// Block (k, part) sums slice x_dir = k over its share of the transverse sites;
+// four sums T_el, T_mag, L_el, L_mag per block, combined per slice in a fixed
+// order by k_projected_final.
 template <int NC, typename R>
-__global__ void __launch_bounds__(256) k_projected_energy(const R *__restrict__ U, const R *__restrict__ Unext,
-                                                          const R *__restrict__ E, const uint8_t *__restrict__ eval,
-                                                          Lat L, int dir, double *__restrict__ out) {
+__global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
+    k_projected_energy(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
+                       const uint8_t *__restrict__ eval, Lat L, int dir, double *__restrict__ part) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
     const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
-    const int k = blockIdx.x;
+    const int k = blockIdx.x, nsplit = gridDim.y;
     const int o1 = (dir + 1) % 3, o2 = (dir + 2) % 3;
     const long nt = L.V / L.n[dir];
     const double area = (double)L.V / (double)L.n[dir];
-    double uf[3];
-    for (int i = 0; i < 3; i++) uf[i] = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i])) / area;
     KSum acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-    for (long t = threadIdx.x; t < nt; t += blockDim.x) {
+    for (long t = (long)blockIdx.y * blockDim.x + threadIdx.x; t < nt; t += (long)nsplit * blockDim.x) {
         int x[3];
         x[dir] = k;
         const int lo = (o1 > o2) ? o1 : o2, hi = (o1 > o2) ? o2 : o1;  // hi = slower of the two
@@ -115,13 +130,15 @@ __global__ void __launch_bounds__(256) k_projected_energy(const R *__restrict__ 
         if (eval && !eval[s]) continue;
         const Nbr nb = neighbours(L, s, x);
         double el_t = 0, el_l = 0, mg_t = 0, mg_l = 0;
+#pragma unroll 1
         for (int j = 0; j < 3; j++) {
+            const double uf = 1.0 / ((L.g * L.a[j]) * (L.g * L.a[j])) / area;
             R e[NA], b0[NA], b1[NA];
             Ep.load_ro(j, s, e);
             field_b<G, R>(Up, L, s, nb, j, b0);
             field_b<G, R>(Unp, L, s, nb, j, b1);
-            const double el = 0.5 * sq<R, NA>(e) * uf[j];
-            const double mg = 0.25 * (sq<R, NA>(b0) + sq<R, NA>(b1)) * uf[j];
+            const double el = 0.5 * sqr<R, NA>(e) * uf;
+            const double mg = 0.25 * (sqr<R, NA>(b0) + sqr<R, NA>(b1)) * uf;
             if (j == dir) { el_l += el; mg_l += mg; } else { el_t += el; mg_t += mg; }
         }
         two_sum_add(acc[0], el_t);
@@ -131,7 +148,23 @@ __global__ void __launch_bounds__(256) k_projected_energy(const R *__restrict__ 
     }
     int q;
     KSum v = block_reduce<4>(acc, q);
-    if (q >= 0) out[(long)q * L.n[dir] + k] = v.s + v.c;
+    if (q >= 0) {
+        const long o = (((long)k * nsplit + blockIdx.y) * 4 + q) * 2;
+        part[o] = v.s;
+        part[o + 1] = v.c;
+    }
+}
+
+__global__ void k_projected_final(const double *__restrict__ part, int nslices, int nsplit, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = q * nslices + k
+    if (i >= 4 * nslices) return;
+    const int q = i / nslices, k = i % nslices;
+    KSum v{0.0, 0.0};
+    for (int b = 0; b < nsplit; b++) {
+        const long o = (((long)k * nsplit + b) * 4 + q) * 2;
+        ksum_merge(v, KSum{part[o], part[o + 1]});
+    }
+    out[(long)q * nslices + k] = v.s + v.c;
 }
 
 template <int NC, typename R>
@@ -173,9 +206,16 @@ void launch_energy_density(Ctx &c, double *out) { OPX_DISPATCH(energy_density_t,
 
 template <int NC, typename R>
 static void projected_energy_t(Ctx &c, int dir, double *out) {
-    k_projected_energy<NC, R><<<c.L.n[dir], 256, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
-                                                                (const R *)c.E, c.eval, c.L, dir, out);
-    c.launches++;
+    // split each slice over enough blocks to fill the GPU, within the partial buffer
+    const int ns = c.L.n[dir];
+    const long nt = c.L.V / ns;
+    int nsplit = (int)std::max<long>(1, std::min<long>(c.red_blocks / ns, nt / RED_THREADS));
+    nsplit = std::min(nsplit, (int)(c.red_blocks * 2 / ns));  // 8 doubles per (slice, split) in 16 * red_blocks
+    nsplit = std::max(nsplit, 1);
+    k_projected_energy<NC, R><<<dim3(ns, nsplit), RED_THREADS, 0, c.stream>>>(
+        (const R *)c.U, (const R *)c.Unext, (const R *)c.E, c.eval, c.L, dir, c.red_part);
+    k_projected_final<<<grid_for(4L * ns, 128), 128, 0, c.stream>>>(c.red_part, ns, nsplit, out);
+    c.launches += 2;
 }
 void launch_projected_energy(Ctx &c, int dir, double *out) { OPX_DISPATCH(projected_energy_t, c, dir, out); }
 

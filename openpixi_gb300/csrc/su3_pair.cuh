@@ -1,0 +1,433 @@
+// su3_pair.cuh -- SU(3) FP32 arithmetic on two sites at once.
+//
+// Every value is a float2 whose lanes belong to two different lattice sites
+// (site A in .x, site B in .y), and every operation is one paired FP32
+// instruction (fma/mul/add .f32x2) for both sites.  The SU(3) leapfrog is
+// issue-bound in scalar FP32 (the FMA pipe is not saturated), so executing the
+// same arithmetic for two sites per instruction halves the issue slots the
+// arithmetic takes.  Control flow is uniform over the two lanes: the
+// exponential's series runs until both lanes have converged and both lanes use
+// the larger scaling exponent.
+//
+// Matrices are 3x3 complex, row-major, real and imaginary parts in separate
+// arrays (the storage order of the links).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace opx {
+namespace pr {
+
+typedef float2 P;
+
+__device__ __forceinline__ P pp(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ P bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ P fma2(P a, P b, P c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ P mul2(P a, P b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ P add2(P a, P b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ P neg2(P a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ P sub2(P a, P b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ P zero2() { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ float maxl(P a) { return fmaxf(a.x, a.y); }
+
+struct M {
+    P r[9], i[9];
+};
+
+__device__ __forceinline__ M mzero() {
+    M m;
+#pragma unroll
+    for (int k = 0; k < 9; k++) { m.r[k] = zero2(); m.i[k] = zero2(); }
+    return m;
+}
+
+// (a b)_{rq} real and imaginary parts; positive and negative products are
+// accumulated separately so that no operand needs a sign change.
+__device__ __forceinline__ void e_mul(const M &a, const M &b, int r, int q, P &re, P &im) {
+    P rp = mul2(a.r[3 * r], b.r[q]);
+    rp = fma2(a.r[3 * r + 1], b.r[3 + q], rp);
+    rp = fma2(a.r[3 * r + 2], b.r[6 + q], rp);
+    P rn = mul2(a.i[3 * r], b.i[q]);
+    rn = fma2(a.i[3 * r + 1], b.i[3 + q], rn);
+    rn = fma2(a.i[3 * r + 2], b.i[6 + q], rn);
+    P ii = mul2(a.r[3 * r], b.i[q]);
+    ii = fma2(a.r[3 * r + 1], b.i[3 + q], ii);
+    ii = fma2(a.r[3 * r + 2], b.i[6 + q], ii);
+    ii = fma2(a.i[3 * r], b.r[q], ii);
+    ii = fma2(a.i[3 * r + 1], b.r[3 + q], ii);
+    ii = fma2(a.i[3 * r + 2], b.r[6 + q], ii);
+    re = sub2(rp, rn);
+    im = ii;
+}
+__device__ __forceinline__ P e_mul_im(const M &a, const M &b, int r, int q) {
+    P ii = mul2(a.r[3 * r], b.i[q]);
+    ii = fma2(a.r[3 * r + 1], b.i[3 + q], ii);
+    ii = fma2(a.r[3 * r + 2], b.i[6 + q], ii);
+    ii = fma2(a.i[3 * r], b.r[q], ii);
+    ii = fma2(a.i[3 * r + 1], b.r[3 + q], ii);
+    ii = fma2(a.i[3 * r + 2], b.r[6 + q], ii);
+    return ii;
+}
+
+// a b
+__device__ __forceinline__ M mul(const M &a, const M &b) {
+    M c;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) e_mul(a, b, r, q, c.r[3 * r + q], c.i[3 * r + q]);
+    return c;
+}
+
+// a b^dagger: re = sum a.r b.r + a.i b.i, im = sum a.i b.r - a.r b.i (b indexed [q][k])
+__device__ __forceinline__ M mul_adj(const M &a, const M &b) {
+    M c;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            P re = mul2(a.r[3 * r], b.r[3 * q]);
+            re = fma2(a.r[3 * r + 1], b.r[3 * q + 1], re);
+            re = fma2(a.r[3 * r + 2], b.r[3 * q + 2], re);
+            re = fma2(a.i[3 * r], b.i[3 * q], re);
+            re = fma2(a.i[3 * r + 1], b.i[3 * q + 1], re);
+            re = fma2(a.i[3 * r + 2], b.i[3 * q + 2], re);
+            P ip = mul2(a.i[3 * r], b.r[3 * q]);
+            ip = fma2(a.i[3 * r + 1], b.r[3 * q + 1], ip);
+            ip = fma2(a.i[3 * r + 2], b.r[3 * q + 2], ip);
+            P in = mul2(a.r[3 * r], b.i[3 * q]);
+            in = fma2(a.r[3 * r + 1], b.i[3 * q + 1], in);
+            in = fma2(a.r[3 * r + 2], b.i[3 * q + 2], in);
+            c.r[3 * r + q] = re;
+            c.i[3 * r + q] = sub2(ip, in);
+        }
+    return c;
+}
+
+// a^dagger b: re = sum a.r b.r + a.i b.i, im = sum a.r b.i - a.i b.r (a indexed [k][r])
+__device__ __forceinline__ M adj_mul(const M &a, const M &b) {
+    M c;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            P re = mul2(a.r[r], b.r[q]);
+            re = fma2(a.r[3 + r], b.r[3 + q], re);
+            re = fma2(a.r[6 + r], b.r[6 + q], re);
+            re = fma2(a.i[r], b.i[q], re);
+            re = fma2(a.i[3 + r], b.i[3 + q], re);
+            re = fma2(a.i[6 + r], b.i[6 + q], re);
+            P ip = mul2(a.r[r], b.i[q]);
+            ip = fma2(a.r[3 + r], b.i[3 + q], ip);
+            ip = fma2(a.r[6 + r], b.i[6 + q], ip);
+            P in = mul2(a.i[r], b.r[q]);
+            in = fma2(a.i[3 + r], b.r[3 + q], in);
+            in = fma2(a.i[6 + r], b.r[6 + q], in);
+            c.r[3 * r + q] = re;
+            c.i[3 * r + q] = sub2(ip, in);
+        }
+    return c;
+}
+
+__device__ __forceinline__ void madd(M &acc, const M &b) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) { acc.r[k] = add2(acc.r[k], b.r[k]); acc.i[k] = add2(acc.i[k], b.i[k]); }
+}
+// acc += f b
+__device__ __forceinline__ void maxpy(M &acc, P f, const M &b) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) { acc.r[k] = fma2(f, b.r[k], acc.r[k]); acc.i[k] = fma2(f, b.i[k], acc.i[k]); }
+}
+
+// x = proj(a b), proj_a(M) = Im tr(lambda_a M); only the entries proj reads
+// are formed: the imaginary diagonal and the six off-diagonal entries.
+__device__ __forceinline__ void proj_mul(const M &a, const M &b, P *x) {
+    const P d0 = e_mul_im(a, b, 0, 0), d1 = e_mul_im(a, b, 1, 1), d2 = e_mul_im(a, b, 2, 2);
+    P r01, i01, r10, i10, r02, i02, r20, i20, r12, i12, r21, i21;
+    e_mul(a, b, 0, 1, r01, i01);
+    e_mul(a, b, 1, 0, r10, i10);
+    e_mul(a, b, 0, 2, r02, i02);
+    e_mul(a, b, 2, 0, r20, i20);
+    e_mul(a, b, 1, 2, r12, i12);
+    e_mul(a, b, 2, 1, r21, i21);
+    x[0] = add2(i01, i10);
+    x[1] = sub2(r01, r10);
+    x[2] = sub2(d0, d1);
+    x[3] = add2(i02, i20);
+    x[4] = sub2(r02, r20);
+    x[5] = add2(i12, i21);
+    x[6] = sub2(r12, r21);
+    x[7] = mul2(sub2(add2(d0, d1), add2(d2, d2)), bc(0.57735026918962576451f));
+}
+
+// exp(i H), H = x^a lambda_a / 2, by the Cayley-Hamilton reduction
+// exp(iH) = f0 + f1 H + f2 H^2 with the scalar series of the scalar SU(3) code
+// (H^3 = c1 H + c0, c1 = tr(H^2)/2, c0 = det H), scaling and squaring above
+// ||H||_F^2 = 1.  H^2 uses the hermitian structure (six distinct entries).
+__device__ __forceinline__ M expi(const P *x) {
+    const P half = bc(0.5f), c2s3 = bc(0.28867513459481288225f);
+    // H: real diagonal d, off-diagonal u = H01, v = H02, w = H12
+    P d0 = fma2(half, x[2], mul2(c2s3, x[7]));
+    P d1 = sub2(mul2(c2s3, x[7]), mul2(half, x[2]));
+    P d2 = mul2(bc(-0.57735026918962576451f), x[7]);
+    P ur = mul2(half, x[0]), ui = mul2(bc(-0.5f), x[1]);
+    P vr = mul2(half, x[3]), vi = mul2(bc(-0.5f), x[4]);
+    P wr = mul2(half, x[5]), wi = mul2(bc(-0.5f), x[6]);
+    P c1 = mul2(x[0], x[0]);
+#pragma unroll
+    for (int a = 1; a < 8; a++) c1 = fma2(x[a], x[a], c1);
+    c1 = mul2(c1, bc(0.25f));
+    int s = 0;
+    float sc = 1.f;
+    const float c1m = maxl(c1);
+    while (2.f * c1m * sc * sc > 1.f && s < 30) { sc *= 0.5f; s++; }
+    if (s) {
+        const P S = bc(sc), S2 = bc(sc * sc);
+        d0 = mul2(d0, S); d1 = mul2(d1, S); d2 = mul2(d2, S);
+        ur = mul2(ur, S); ui = mul2(ui, S); vr = mul2(vr, S); vi = mul2(vi, S); wr = mul2(wr, S); wi = mul2(wi, S);
+        c1 = mul2(c1, S2);
+    }
+    const P uu = fma2(ur, ur, mul2(ui, ui)), vv = fma2(vr, vr, mul2(vi, vi)), ww = fma2(wr, wr, mul2(wi, wi));
+    // det H = d0 (d1 d2 - |w|^2) - d1 |v|^2 - d2 |u|^2 + 2 Re(u w conj(v))
+    P c0 = mul2(d0, sub2(mul2(d1, d2), ww));
+    c0 = sub2(c0, mul2(d1, vv));
+    c0 = sub2(c0, mul2(d2, uu));
+    P re_uwv = fma2(ur, fma2(wr, vr, mul2(wi, vi)), mul2(ui, sub2(mul2(wr, vi), mul2(wi, vr))));
+    c0 = fma2(bc(2.f), re_uwv, c0);
+    // series
+    P al = bc(1.f), be = zero2(), ga = zero2();
+    float t = 1.f;
+    P f0r = bc(1.f), f0i = zero2(), f1r = zero2(), f1i = zero2(), f2r = zero2(), f2i = zero2();
+    const P two_c1 = add2(c1, c1);
+    const P nrm = pp(sqrtf(two_c1.x), sqrtf(two_c1.y));
+    P bound = bc(1.f);
+    for (int k = 1; k < 40; k++) {
+        const P nal = mul2(c0, ga), nbe = fma2(c1, ga, al);
+        ga = be;
+        al = nal;
+        be = nbe;
+        t = t / (float)k;
+        const P T = bc(t), mT = bc(-t);
+        switch (k & 3) {
+        case 0: f0r = fma2(T, al, f0r); f1r = fma2(T, be, f1r); f2r = fma2(T, ga, f2r); break;
+        case 1: f0i = fma2(T, al, f0i); f1i = fma2(T, be, f1i); f2i = fma2(T, ga, f2i); break;
+        case 2: f0r = fma2(mT, al, f0r); f1r = fma2(mT, be, f1r); f2r = fma2(mT, ga, f2r); break;
+        default: f0i = fma2(mT, al, f0i); f1i = fma2(mT, be, f1i); f2i = fma2(mT, ga, f2i); break;
+        }
+        bound = mul2(bound, nrm);
+        if (maxl(bound) * t < 5.9604645e-08f * 0.01f) break;
+    }
+    // Q = H^2 (hermitian)
+    const P q00 = add2(fma2(d0, d0, uu), vv), q11 = add2(fma2(d1, d1, uu), ww), q22 = add2(fma2(d2, d2, vv), ww);
+    const P s01 = add2(d0, d1), s02 = add2(d0, d2), s12 = add2(d1, d2);
+    // Q01 = u (d0 + d1) + v conj(w)
+    const P q01r = fma2(ur, s01, fma2(vr, wr, mul2(vi, wi)));
+    const P q01i = fma2(ui, s01, sub2(mul2(vi, wr), mul2(vr, wi)));
+    // Q02 = v (d0 + d2) + u w
+    const P q02r = fma2(vr, s02, sub2(mul2(ur, wr), mul2(ui, wi)));
+    const P q02i = fma2(vi, s02, fma2(ur, wi, mul2(ui, wr)));
+    // Q12 = w (d1 + d2) + conj(u) v
+    const P q12r = fma2(wr, s12, fma2(ur, vr, mul2(ui, vi)));
+    const P q12i = fma2(wi, s12, sub2(mul2(ur, vi), mul2(ui, vr)));
+    M W;
+    // diagonal: f0 + f1 d + f2 q
+    W.r[0] = fma2(f2r, q00, fma2(f1r, d0, f0r));
+    W.i[0] = fma2(f2i, q00, fma2(f1i, d0, f0i));
+    W.r[4] = fma2(f2r, q11, fma2(f1r, d1, f0r));
+    W.i[4] = fma2(f2i, q11, fma2(f1i, d1, f0i));
+    W.r[8] = fma2(f2r, q22, fma2(f1r, d2, f0r));
+    W.i[8] = fma2(f2i, q22, fma2(f1i, d2, f0i));
+    // upper entry z = f1 h + f2 q, lower entry f1 conj(h) + f2 conj(q)
+    auto off = [&](P hr, P hi, P qr, P qi, P &ur_, P &ui_, P &lr_, P &li_) {
+        const P a = fma2(f1r, hr, mul2(f2r, qr));  // f1r hr + f2r qr
+        const P b = fma2(f1i, hi, mul2(f2i, qi));  // f1i hi + f2i qi
+        const P c = fma2(f1r, hi, mul2(f2r, qi));  // f1r hi + f2r qi
+        const P e = fma2(f1i, hr, mul2(f2i, qr));  // f1i hr + f2i qr
+        ur_ = sub2(a, b);
+        ui_ = add2(c, e);
+        lr_ = add2(a, b);
+        li_ = sub2(e, c);
+    };
+    off(ur, ui, q01r, q01i, W.r[1], W.i[1], W.r[3], W.i[3]);
+    off(vr, vi, q02r, q02i, W.r[2], W.i[2], W.r[6], W.i[6]);
+    off(wr, wi, q12r, q12i, W.r[5], W.i[5], W.r[7], W.i[7]);
+    for (int k = 0; k < s; k++) W = mul(W, W);
+    return W;
+}
+
+// Gram-Schmidt on rows 0 and 1; row 2 = conj(row0 x row1)
+__device__ __forceinline__ void reunit(M &m) {
+    P n0 = mul2(m.r[0], m.r[0]);
+    n0 = fma2(m.i[0], m.i[0], n0);
+#pragma unroll
+    for (int k = 1; k < 3; k++) { n0 = fma2(m.r[k], m.r[k], n0); n0 = fma2(m.i[k], m.i[k], n0); }
+    const P inv0 = pp(1.f / sqrtf(n0.x), 1.f / sqrtf(n0.y));
+#pragma unroll
+    for (int k = 0; k < 3; k++) { m.r[k] = mul2(m.r[k], inv0); m.i[k] = mul2(m.i[k], inv0); }
+    P pr_ = zero2(), pip = zero2(), pin = zero2();
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        pr_ = fma2(m.r[k], m.r[3 + k], pr_);
+        pr_ = fma2(m.i[k], m.i[3 + k], pr_);
+        pip = fma2(m.r[k], m.i[3 + k], pip);
+        pin = fma2(m.i[k], m.r[3 + k], pin);
+    }
+    const P pi_ = sub2(pip, pin), npr = neg2(pr_), npi = neg2(pi_);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        // row1 -= p row0
+        const P nr = fma2(npr, m.r[k], fma2(pi_, m.i[k], m.r[3 + k]));
+        const P ni = fma2(npr, m.i[k], fma2(npi, m.r[k], m.i[3 + k]));
+        m.r[3 + k] = nr;
+        m.i[3 + k] = ni;
+    }
+    P n1 = mul2(m.r[3], m.r[3]);
+    n1 = fma2(m.i[3], m.i[3], n1);
+#pragma unroll
+    for (int k = 4; k < 6; k++) { n1 = fma2(m.r[k], m.r[k], n1); n1 = fma2(m.i[k], m.i[k], n1); }
+    const P inv1 = pp(1.f / sqrtf(n1.x), 1.f / sqrtf(n1.y));
+#pragma unroll
+    for (int k = 3; k < 6; k++) { m.r[k] = mul2(m.r[k], inv1); m.i[k] = mul2(m.i[k], inv1); }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int a = (k + 1) % 3, b = (k + 2) % 3;
+        const P xr = sub2(sub2(mul2(m.r[a], m.r[3 + b]), mul2(m.i[a], m.i[3 + b])),
+                          sub2(mul2(m.r[b], m.r[3 + a]), mul2(m.i[b], m.i[3 + a])));
+        const P xi = sub2(fma2(m.r[a], m.i[3 + b], mul2(m.i[a], m.r[3 + b])),
+                          fma2(m.r[b], m.i[3 + a], mul2(m.i[b], m.r[3 + a])));
+        m.r[6 + k] = xr;
+        m.i[6 + k] = neg2(xi);
+    }
+}
+
+// Warp-blocked link loads and stores for the two sites (layout of lattice.cuh).
+// I is the index type: 32-bit when every link offset fits (54 V < 2^31).
+template <typename I> __device__ __forceinline__ I loff(I nblk, int d, I s) {
+    return ((I)d * nblk + (s >> 5)) * (I)576 + (s & 31);
+}
+template <typename I>
+__device__ __forceinline__ M load(const float *__restrict__ U, I nblk, int d, I sa, I sb) {
+    const float *a = U + loff<I>(nblk, d, sa);
+    const float *b = U + loff<I>(nblk, d, sb);
+    M m;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        m.r[k] = pp(__ldg(a + 32 * k), __ldg(b + 32 * k));
+        m.i[k] = pp(__ldg(a + 32 * (9 + k)), __ldg(b + 32 * (9 + k)));
+    }
+    return m;
+}
+template <typename I>
+__device__ __forceinline__ void store(float *__restrict__ U, I nblk, int d, I sa, I sb, bool va, bool vb, const M &m) {
+    float *a = U + loff<I>(nblk, d, sa);
+    float *b = U + loff<I>(nblk, d, sb);
+    if (va) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) { a[32 * k] = m.r[k].x; a[32 * (9 + k)] = m.i[k].x; }
+    }
+    if (vb) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) { b[32 * k] = m.r[k].y; b[32 * (9 + k)] = m.i[k].y; }
+    }
+}
+
+// acc += f a b^dagger (the forward staple's last product folded into the sum)
+__device__ __forceinline__ void acc_mul_adj(M &acc, P f, const M &a, const M &b) {
+    const M c = mul_adj(a, b);
+    maxpy(acc, f, c);
+}
+// acc += f a^dagger b
+__device__ __forceinline__ void acc_adj_mul(M &acc, P f, const M &a, const M &b) {
+    const M c = adj_mul(a, b);
+    maxpy(acc, f, c);
+}
+
+// Periodic shift by one in direction d (runtime), orientation o, given the
+// coordinate xd of s along d.
+template <typename I> __device__ __forceinline__ I shift(const Lat &L, I s, int xd, int d, int o) {
+    const int nd = d == 0 ? L.n[0] : (d == 1 ? L.n[1] : L.n[2]);
+    const I st = d == 0 ? (I)L.stride[0] : (d == 1 ? (I)L.stride[1] : (I)1);
+    if (o > 0) return xd == nd - 1 ? s - (I)(nd - 1) * st : s + st;
+    return xd == 0 ? s + (I)(nd - 1) * st : s - st;
+}
+template <typename I> __device__ __forceinline__ void coords(const Lat &L, I s, int *x) {
+    const I t = s / (I)L.n[2];
+    x[2] = (int)(s - t * (I)L.n[2]);
+    const I u = t / (I)L.n[1];
+    x[1] = (int)(t - u * (I)L.n[1]);
+    x[0] = (int)u;
+}
+
+}  // namespace pr
+
+// FastTYMSolver.CombinedUpdate for SU(3) FP32 at sites sa and sb; a lane
+// whose flag (va, vb) is false computes but stores nothing (a site past the end
+// of the lattice or an inactive cell).  Same equations and staple order as
+// update_site in leapfrog.cuh.
+template <typename I, bool HAS_J, bool REUNIT>
+__device__ __forceinline__ void update_site_pair(const float *__restrict__ U, float *__restrict__ E,
+                                                 const float *__restrict__ J, float *__restrict__ Unext,
+                                                 const Lat &L, I sa, I sb, bool va, bool vb) {
+    using namespace pr;
+    const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
+    int xa[3], xb[3];
+    coords<I>(L, sa, xa);
+    coords<I>(L, sb, xb);
+    const P dt = bc(L.dtf), mdt = bc(-L.dtf);
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) {
+        const int xia = pick(xa[0], xa[1], xa[2], i), xib = pick(xb[0], xb[1], xb[2], i);
+        const I pia = shift<I>(L, sa, xia, i, +1), pib = shift<I>(L, sb, xib, i, +1);  // x + i
+        M S = mzero();
+#pragma unroll 1
+        for (int jj = 1; jj < 3; jj++) {
+            const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
+            const int xja = pick(xa[0], xa[1], xa[2], j), xjb = pick(xb[0], xb[1], xb[2], j);
+            const P f = bc(LatR<float>::inva2(L, j));
+            {
+                // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
+                const I pja = shift<I>(L, sa, xja, j, +1), pjb = shift<I>(L, sb, xjb, j, +1);
+                const M T = mul_adj(load<I>(U, nblk, j, pia, pib), load<I>(U, nblk, i, pja, pjb));
+                acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
+            }
+            {
+                // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
+                const I mja = shift<I>(L, sa, xja, j, -1), mjb = shift<I>(L, sb, xjb, j, -1);
+                const I pimja = shift<I>(L, pia, xja, j, -1), pimjb = shift<I>(L, pib, xjb, j, -1);
+                const M C = mul(load<I>(U, nblk, i, mja, mjb), load<I>(U, nblk, j, pimja, pimjb));
+                acc_adj_mul(S, f, C, load<I>(U, nblk, j, mja, mjb));
+            }
+        }
+        const M Ui = load<I>(U, nblk, i, sa, sb);
+        P p[8], e[8];
+        proj_mul(Ui, S, p);
+        const I eo = (I)i * 8 * V;
+        const float *ea = E + eo + sa, *eb = E + eo + sb;
+#pragma unroll
+        for (int a = 0; a < 8; a++) e[a] = fma2(p[a], dt, pp(ea[(I)a * V], eb[(I)a * V]));
+        if (HAS_J) {
+            const float *ja = J + eo + sa, *jb = J + eo + sb;
+            const P jf = bc(LatR<float>::jfac(L, i));
+#pragma unroll
+            for (int a = 0; a < 8; a++) e[a] = fma2(pp(__ldg(ja + (I)a * V), __ldg(jb + (I)a * V)), jf, e[a]);
+        }
+        float *wa = E + eo + sa, *wb = E + eo + sb;
+        if (va) {
+#pragma unroll
+            for (int a = 0; a < 8; a++) wa[(I)a * V] = e[a].x;
+        }
+        if (vb) {
+#pragma unroll
+            for (int a = 0; a < 8; a++) wb[(I)a * V] = e[a].y;
+        }
+        P v[8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) v[a] = mul2(mdt, e[a]);
+        M Vn = mul(expi(v), Ui);
+        if (REUNIT) reunit(Vn);
+        store<I>(Unext, nblk, i, sa, sb, va, vb, Vn);
+    }
+}
+
+}  // namespace opx
