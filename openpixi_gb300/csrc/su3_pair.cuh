@@ -21,6 +21,13 @@ namespace pr {
 
 typedef float2 P;
 
+// 1/k for the exponential series (t_k = t_{k-1} / k), read with a uniform index
+static __constant__ float c_inv_k[40] = {
+    0.f,         1.f,         1.f / 2,  1.f / 3,  1.f / 4,  1.f / 5,  1.f / 6,  1.f / 7,  1.f / 8,  1.f / 9,
+    1.f / 10,    1.f / 11,    1.f / 12, 1.f / 13, 1.f / 14, 1.f / 15, 1.f / 16, 1.f / 17, 1.f / 18, 1.f / 19,
+    1.f / 20,    1.f / 21,    1.f / 22, 1.f / 23, 1.f / 24, 1.f / 25, 1.f / 26, 1.f / 27, 1.f / 28, 1.f / 29,
+    1.f / 30,    1.f / 31,    1.f / 32, 1.f / 33, 1.f / 34, 1.f / 35, 1.f / 36, 1.f / 37, 1.f / 38, 1.f / 39};
+
 __device__ __forceinline__ P pp(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ P bc(float a) { return make_float2(a, a); }
 __device__ __forceinline__ P fma2(P a, P b, P c) { return __ffma2_rn(a, b, c); }
@@ -70,63 +77,83 @@ __device__ __forceinline__ P e_mul_im(const M &a, const M &b, int r, int q) {
     return ii;
 }
 
+// The products below run k-outer: every k adds one term to all nine output
+// entries, so eighteen independent accumulator chains interleave and the FMA
+// latency is covered within one thread.  One operand's sign-flipped copy
+// replaces the subtractions.
+
 // a b
 __device__ __forceinline__ M mul(const M &a, const M &b) {
     M c;
+    P nai[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) nai[k] = neg2(a.i[k]);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
-        for (int q = 0; q < 3; q++) e_mul(a, b, r, q, c.r[3 * r + q], c.i[3 * r + q]);
+        for (int q = 0; q < 3; q++) {
+            c.r[3 * r + q] = fma2(nai[3 * r], b.i[q], mul2(a.r[3 * r], b.r[q]));
+            c.i[3 * r + q] = fma2(a.i[3 * r], b.r[q], mul2(a.r[3 * r], b.i[q]));
+        }
+#pragma unroll
+    for (int k = 1; k < 3; k++)
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                c.r[3 * r + q] = fma2(nai[3 * r + k], b.i[3 * k + q], fma2(a.r[3 * r + k], b.r[3 * k + q], c.r[3 * r + q]));
+                c.i[3 * r + q] = fma2(a.i[3 * r + k], b.r[3 * k + q], fma2(a.r[3 * r + k], b.i[3 * k + q], c.i[3 * r + q]));
+            }
     return c;
 }
 
-// a b^dagger: re = sum a.r b.r + a.i b.i, im = sum a.i b.r - a.r b.i (b indexed [q][k])
+// a b^dagger: (b^dagger)_{kq} = conj(b_{qk})
 __device__ __forceinline__ M mul_adj(const M &a, const M &b) {
     M c;
+    P nbi[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) nbi[k] = neg2(b.i[k]);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            P re = mul2(a.r[3 * r], b.r[3 * q]);
-            re = fma2(a.r[3 * r + 1], b.r[3 * q + 1], re);
-            re = fma2(a.r[3 * r + 2], b.r[3 * q + 2], re);
-            re = fma2(a.i[3 * r], b.i[3 * q], re);
-            re = fma2(a.i[3 * r + 1], b.i[3 * q + 1], re);
-            re = fma2(a.i[3 * r + 2], b.i[3 * q + 2], re);
-            P ip = mul2(a.i[3 * r], b.r[3 * q]);
-            ip = fma2(a.i[3 * r + 1], b.r[3 * q + 1], ip);
-            ip = fma2(a.i[3 * r + 2], b.r[3 * q + 2], ip);
-            P in = mul2(a.r[3 * r], b.i[3 * q]);
-            in = fma2(a.r[3 * r + 1], b.i[3 * q + 1], in);
-            in = fma2(a.r[3 * r + 2], b.i[3 * q + 2], in);
-            c.r[3 * r + q] = re;
-            c.i[3 * r + q] = sub2(ip, in);
+            c.r[3 * r + q] = fma2(a.i[3 * r], b.i[3 * q], mul2(a.r[3 * r], b.r[3 * q]));
+            c.i[3 * r + q] = fma2(a.r[3 * r], nbi[3 * q], mul2(a.i[3 * r], b.r[3 * q]));
         }
+#pragma unroll
+    for (int k = 1; k < 3; k++)
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                c.r[3 * r + q] = fma2(a.i[3 * r + k], b.i[3 * q + k], fma2(a.r[3 * r + k], b.r[3 * q + k], c.r[3 * r + q]));
+                c.i[3 * r + q] = fma2(a.r[3 * r + k], nbi[3 * q + k], fma2(a.i[3 * r + k], b.r[3 * q + k], c.i[3 * r + q]));
+            }
     return c;
 }
 
-// a^dagger b: re = sum a.r b.r + a.i b.i, im = sum a.r b.i - a.i b.r (a indexed [k][r])
+// a^dagger b: (a^dagger)_{rk} = conj(a_{kr})
 __device__ __forceinline__ M adj_mul(const M &a, const M &b) {
     M c;
+    P nai[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) nai[k] = neg2(a.i[k]);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            P re = mul2(a.r[r], b.r[q]);
-            re = fma2(a.r[3 + r], b.r[3 + q], re);
-            re = fma2(a.r[6 + r], b.r[6 + q], re);
-            re = fma2(a.i[r], b.i[q], re);
-            re = fma2(a.i[3 + r], b.i[3 + q], re);
-            re = fma2(a.i[6 + r], b.i[6 + q], re);
-            P ip = mul2(a.r[r], b.i[q]);
-            ip = fma2(a.r[3 + r], b.i[3 + q], ip);
-            ip = fma2(a.r[6 + r], b.i[6 + q], ip);
-            P in = mul2(a.i[r], b.r[q]);
-            in = fma2(a.i[3 + r], b.r[3 + q], in);
-            in = fma2(a.i[6 + r], b.r[6 + q], in);
-            c.r[3 * r + q] = re;
-            c.i[3 * r + q] = sub2(ip, in);
+            c.r[3 * r + q] = fma2(a.i[r], b.i[q], mul2(a.r[r], b.r[q]));
+            c.i[3 * r + q] = fma2(nai[r], b.r[q], mul2(a.r[r], b.i[q]));
         }
+#pragma unroll
+    for (int k = 1; k < 3; k++)
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                c.r[3 * r + q] = fma2(a.i[3 * k + r], b.i[3 * k + q], fma2(a.r[3 * k + r], b.r[3 * k + q], c.r[3 * r + q]));
+                c.i[3 * r + q] = fma2(nai[3 * k + r], b.r[3 * k + q], fma2(a.r[3 * k + r], b.i[3 * k + q], c.i[3 * r + q]));
+            }
     return c;
 }
 
@@ -207,7 +234,7 @@ __device__ __forceinline__ M expi(const P *x) {
         ga = be;
         al = nal;
         be = nbe;
-        t = t / (float)k;
+        t = t * c_inv_k[k];
         const P T = bc(t), mT = bc(-t);
         switch (k & 3) {
         case 0: f0r = fma2(T, al, f0r); f1r = fma2(T, be, f1r); f2r = fma2(T, ga, f2r); break;
