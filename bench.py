@@ -58,6 +58,29 @@ SEED = 20261203
 METRIC = "link-updates/s"
 
 
+class nvtx_range:
+    """NVTX range around a bench phase (ncu --nvtx --nvtx-include <name>/ selects
+    the kernels launched inside it); a no-op when NVTX is unavailable."""
+
+    def __init__(self, name):
+        self.name = name
+        try:
+            import torch.cuda.nvtx as nv
+            self.nv = nv
+        except Exception:
+            self.nv = None
+
+    def __enter__(self):
+        if self.nv is not None:
+            self.nv.range_push(self.name)
+        return self
+
+    def __exit__(self, *exc):
+        if self.nv is not None:
+            self.nv.range_pop()
+        return False
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
         int(os.environ.get("LOCAL_RANK", "0"))
@@ -437,8 +460,9 @@ def main():
     l0 = h.kernel_launches
     dist.barrier()
     h.synchronize()
-    ms = h.time_steps(args.steps)
-    h.synchronize()
+    with nvtx_range("timed_steps"):
+        ms = h.time_steps(args.steps)
+        h.synchronize()
     dist.barrier()
     launches = h.kernel_launches - l0
     clk = clocks.stop()
@@ -464,8 +488,9 @@ def main():
 
     # ---- the BulkQuantities reduction (one pass: E^2, B^2 from U and Unext, Gauss, rho^2)
     h.set_profiling(True)
-    for _ in range(10):
-        h.reduce()
+    with nvtx_range("reduce"):
+        for _ in range(10):
+            h.reduce()
     rms, rn = h.phase_times()
     h.set_profiling(False)
     reduce_ms = rms[N.PHASE_DIA] / max(rn[N.PHASE_DIA], 1)

@@ -15,6 +15,7 @@
 #include "internal.h"
 #include "ksum.cuh"
 #include "observables.cuh"
+#include "su3_pair.cuh"
 
 namespace opx {
 
@@ -55,10 +56,145 @@ __global__ void k_bulk_final(const double *__restrict__ part, int nblocks, doubl
     if (lane == 0) out[q] = v.s + v.c;
 }
 
+// SU(3) FP32: two sites per thread in paired FP32 instructions (the
+// arithmetic of bulk_accumulate for sites sa and sb = sa + 32; the two lanes
+// are summed into the thread's partial sums).
+template <typename I>
+__global__ void __launch_bounds__(RED_THREADS, 3)
+    k_bulk_partial_su3f_pair(const float *__restrict__ U, const float *__restrict__ Unext,
+                             const float *__restrict__ E, const float *__restrict__ rho,
+                             const uint8_t *__restrict__ eval, Lat L, double *__restrict__ part) {
+    using namespace pr;
+    const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
+    const I npairs = (I)(((L.V + 63) >> 6) << 5);
+    KSum acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) acc[q] = KSum{0.0, 0.0};
+    double p[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) p[q] = 0.0;
+    int run = 0;
+    for (I t = (I)blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += (I)gridDim.x * blockDim.x) {
+        const I sa = ((t >> 5) << 6) + (t & 31);
+        if (sa >= V) continue;
+        I sb = sa + 32;
+        bool vb = sb < V;
+        if (!vb) sb = sa;
+        const bool wa = !eval || eval[sa];
+        const bool wb = vb && (!eval || eval[sb]);
+        if (!wa && !wb) continue;
+        int xa[3], xb[3];
+        coords<I>(L, sa, xa);
+        coords<I>(L, sb, xb);
+        auto widen = [&](P v) { return (wa ? (double)v.x : 0.0) + (wb ? (double)v.y : 0.0); };
+#pragma unroll 1
+        for (int d = 0; d < 3; d++) {
+            // E^2 of link d
+            const I eo = (I)d * 8 * V;
+            P e[8];
+#pragma unroll
+            for (int a = 0; a < 8; a++) e[a] = pp(__ldg(E + eo + (I)a * V + sa), __ldg(E + eo + (I)a * V + sb));
+            P se = mul2(e[0], e[0]);
+#pragma unroll
+            for (int a = 1; a < 8; a++) se = fma2(e[a], e[a], se);
+            // B_d from U and Unext: U_j(x) U_k(x+j) U_j(x+k)^dagger U_k(x)^dagger, (d, j, k) cyclic
+            const int j = d + 1 >= 3 ? d - 2 : d + 1, k = d + 2 >= 3 ? d - 1 : d + 2;
+            const I pja = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], j), j, +1);
+            const I pjb = shift<I>(L, sb, pick(xb[0], xb[1], xb[2], j), j, +1);
+            const I pka = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], k), k, +1);
+            const I pkb = shift<I>(L, sb, pick(xb[0], xb[1], xb[2], k), k, +1);
+            const P bf = bc(LatR<float>::bfac(L, d));
+            P sb2 = zero2();
+#pragma unroll 1
+            for (int tt = 0; tt < 2; tt++) {
+                const float *W = tt == 0 ? U : Unext;
+                const M Pq = mul_adj(mul_adj(mul(load<I>(W, nblk, j, sa, sb), load<I>(W, nblk, k, pja, pjb)),
+                                             load<I>(W, nblk, j, pka, pkb)),
+                                     load<I>(W, nblk, k, sa, sb));
+                P b[8];
+                proj(Pq, b);
+#pragma unroll
+                for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); sb2 = fma2(b[a], b[a], sb2); }
+            }
+            const double ev = widen(se), bv = widen(sb2);
+            if (d == 0) { p[0] += ev; p[3] += bv; }
+            else if (d == 1) { p[1] += ev; p[4] += bv; }
+            else { p[2] += ev; p[5] += bv; }
+        }
+        // Gauss: sum_i [E_i(x) - U_i(x-i)^dagger E_i(x-i) U_i(x-i)] gfac_i - rho(x)
+        P gs[8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) gs[a] = zero2();
+#pragma unroll 1
+        for (int i = 0; i < 3; i++) {
+            const I mia = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], i), i, -1);
+            const I mib = shift<I>(L, sb, pick(xb[0], xb[1], xb[2], i), i, -1);
+            const I eo = (I)i * 8 * V;
+            P e0[8], e1[8], tv[8];
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                e0[a] = pp(__ldg(E + eo + (I)a * V + sa), __ldg(E + eo + (I)a * V + sb));
+                e1[a] = pp(__ldg(E + eo + (I)a * V + mia), __ldg(E + eo + (I)a * V + mib));
+            }
+            const M Ub = load<I>(U, nblk, i, mia, mib);
+            herm_gen(mul(adj_mul(Ub, herm(e1)), Ub), tv);
+            const P gf = bc(LatR<float>::gfac(L, i));
+#pragma unroll
+            for (int a = 0; a < 8; a++) gs[a] = fma2(sub2(e0[a], tv[a]), gf, gs[a]);
+        }
+        if (rho) {
+            P r2 = zero2();
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const P r = pp(__ldg(rho + (I)a * V + sa), __ldg(rho + (I)a * V + sb));
+                gs[a] = sub2(gs[a], r);
+                r2 = fma2(r, r, r2);
+            }
+            p[7] += widen(r2);
+        }
+        P g2 = mul2(gs[0], gs[0]);
+#pragma unroll
+        for (int a = 1; a < 8; a++) g2 = fma2(gs[a], gs[a], g2);
+        p[6] += widen(g2);
+        if (++run == 16) {
+#pragma unroll
+            for (int q = 0; q < NQ; q++) { two_sum_add(acc[q], p[q]); p[q] = 0.0; }
+            run = 0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; q++) two_sum_add(acc[q], p[q]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const double uf = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
+        acc[i].s *= uf; acc[i].c *= uf;
+        acc[3 + i].s *= 0.5 * uf; acc[3 + i].c *= 0.5 * uf;
+    }
+    int q;
+    KSum v = block_reduce<NQ>(acc, q);
+    if (q >= 0) {
+        part[((long)blockIdx.x * NQ + q) * 2] = v.s;
+        part[((long)blockIdx.x * NQ + q) * 2 + 1] = v.c;
+    }
+}
+
 int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
 
 template <int NC, typename R>
 static void bulk_t(Ctx &c) {
+    if (NC == 3 && sizeof(R) == 4 && c.pair_kernel) {
+        if (link_elems(c.L.V, 18) < (1L << 31) - 64)
+            k_bulk_partial_su3f_pair<int><<<c.red_blocks, RED_THREADS, 0, c.stream>>>(
+                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
+                c.red_part);
+        else
+            k_bulk_partial_su3f_pair<long><<<c.red_blocks, RED_THREADS, 0, c.stream>>>(
+                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
+                c.red_part);
+        k_bulk_final<<<1, 32 * NQ, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
+        c.launches += 2;
+        return;
+    }
     k_bulk_partial<NC, R><<<c.red_blocks, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
                                                                      (const R *)c.E, (const R *)c.rho, c.eval, c.L,
                                                                      c.red_part);

@@ -328,6 +328,44 @@ __device__ __forceinline__ void reunit(M &m) {
     }
 }
 
+// H = x^a lambda_a / 2 as a matrix, and its generator components x^a = tr(lambda_a H)
+__device__ __forceinline__ M herm(const P *x) {
+    const P half = bc(0.5f), mhalf = bc(-0.5f), c2s3 = bc(0.28867513459481288225f);
+    M h;
+    h.r[0] = fma2(half, x[2], mul2(c2s3, x[7]));
+    h.r[4] = sub2(mul2(c2s3, x[7]), mul2(half, x[2]));
+    h.r[8] = mul2(bc(-0.57735026918962576451f), x[7]);
+    h.i[0] = h.i[4] = h.i[8] = zero2();
+    h.r[1] = h.r[3] = mul2(half, x[0]);
+    h.i[1] = mul2(mhalf, x[1]); h.i[3] = mul2(half, x[1]);
+    h.r[2] = h.r[6] = mul2(half, x[3]);
+    h.i[2] = mul2(mhalf, x[4]); h.i[6] = mul2(half, x[4]);
+    h.r[5] = h.r[7] = mul2(half, x[5]);
+    h.i[5] = mul2(mhalf, x[6]); h.i[7] = mul2(half, x[6]);
+    return h;
+}
+__device__ __forceinline__ void herm_gen(const M &h, P *x) {
+    x[0] = add2(h.r[1], h.r[3]);
+    x[1] = sub2(h.i[3], h.i[1]);
+    x[2] = sub2(h.r[0], h.r[4]);
+    x[3] = add2(h.r[2], h.r[6]);
+    x[4] = sub2(h.i[6], h.i[2]);
+    x[5] = add2(h.r[5], h.r[7]);
+    x[6] = sub2(h.i[7], h.i[5]);
+    x[7] = mul2(sub2(add2(h.r[0], h.r[4]), add2(h.r[8], h.r[8])), bc(0.57735026918962576451f));
+}
+// proj(M) for a whole matrix
+__device__ __forceinline__ void proj(const M &m, P *x) {
+    x[0] = add2(m.i[1], m.i[3]);
+    x[1] = sub2(m.r[1], m.r[3]);
+    x[2] = sub2(m.i[0], m.i[4]);
+    x[3] = add2(m.i[2], m.i[6]);
+    x[4] = sub2(m.r[2], m.r[6]);
+    x[5] = add2(m.i[5], m.i[7]);
+    x[6] = sub2(m.r[5], m.r[7]);
+    x[7] = mul2(sub2(add2(m.i[0], m.i[4]), add2(m.i[8], m.i[8])), bc(0.57735026918962576451f));
+}
+
 // Warp-blocked link loads and stores for the two sites (layout of lattice.cuh).
 // I is the index type: 32-bit when every link offset fits (54 V < 2^31).
 template <typename I> __device__ __forceinline__ I loff(I nblk, int d, I s) {
