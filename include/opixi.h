@@ -148,6 +148,11 @@ int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count);
  * 4 rows of dims[dir] doubles: T_el, T_mag, L_el, L_mag */
 int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count);
 /* Grid.getGaussConstraint at every cell (Grid.java:944-968), generator components [V][ngen] */
+/* ProjectedEnergyDensity.PoyntingComputation (ProjectedEnergyDensity.java:182-279):
+ * out [2][dims[dir]]: the longitudinal Poynting vector averaged in space and
+ * time, and only time-averaged.  SU(2) handles (the reference's SU(3) algebra
+ * has no scalar product and throws); every cell counts, as in the reference. */
+int opx_projected_poynting(opx_ctx *ctx, int dir, double *host_out, size_t count);
 int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count);
 
 /* ---- CPIC (physics/grid/CGCParticleInterpolationNGP.java,

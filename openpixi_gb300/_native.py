@@ -42,7 +42,7 @@ EXPORTED = [
     "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
     "opx_batch_kernel_launches",
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
-    "opx_particles_count",
+    "opx_particles_count", "opx_projected_poynting",
 ]
 
 
@@ -142,6 +142,7 @@ def load(path=None):
         "opx_batch_kernel_launches": (C.c_long, [vp]),
         "opx_cgc_mv": (C.c_int, [vp, vp, C.c_int]),
         "opx_particles_count": (C.c_long, [vp]),
+        "opx_projected_poynting": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
         "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
@@ -271,6 +272,11 @@ class Handle:
         out = np.empty(4 * self.dims[d] if 0 <= int(d) < 3 else 1)
         self.check(self.L.opx_projected_energy(self.h, int(d), ptr(out), out.size))
         return out.reshape(4, self.dims[d])
+
+    def projected_poynting(self, d):
+        out = np.empty(2 * self.dims[d] if 0 <= int(d) < 3 else 1)
+        self.check(self.L.opx_projected_poynting(self.h, int(d), ptr(out), out.size))
+        return out.reshape(2, self.dims[d])
 
     def gauss_field(self):
         out = np.empty((self.V, self.ngen))

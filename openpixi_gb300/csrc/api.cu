@@ -417,6 +417,24 @@ int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) 
     return sync_check(c, "opx_projected_energy");
 }
 
+int opx_projected_poynting(opx_ctx *ctx, int dir, double *host_out, size_t count) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (dir < 0 || dir > 2) { c.err = "opx_projected_poynting: dir must be 0, 1 or 2"; return OPX_ERR_INVALID; }
+    if (c.nc != 2) {
+        c.err = "opx_projected_poynting: SU(2) only (the reference's SU(3) algebra has no scalar product)";
+        return OPX_ERR_UNSUPPORTED;
+    }
+    const size_t n = 2 * (size_t)c.L.n[dir];
+    if (!host_out || count != n) { c.err = "opx_projected_poynting: output must hold 2*dims[dir] doubles"; return OPX_ERR_INVALID; }
+    int rc = ensure_staging(c, n);
+    if (rc) return rc;
+    rc = launch_projected_poynting(c, dir, c.staging);
+    if (rc) return rc;
+    cudaMemcpyAsync(host_out, c.staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
+    return sync_check(c, "opx_projected_poynting");
+}
+
 int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count) {
     API_CHECK(ctx);
     Ctx &c = ctx->c;

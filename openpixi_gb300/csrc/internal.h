@@ -72,6 +72,7 @@ void launch_bulk(Ctx &c);  // result in c.red_out[0..7]
 int reduction_blocks(long V);
 void launch_energy_density(Ctx &c, double *dev_out);
 void launch_projected_energy(Ctx &c, int dir, double *dev_out);
+int launch_projected_poynting(Ctx &c, int dir, double *dev_out);  // SU(2) only
 void launch_gauss_field(Ctx &c, double *dev_out);
 // ---- conversions (convert_kernels.cu) ----
 void launch_links_from_ref(Ctx &c, const double *src, void *dst);

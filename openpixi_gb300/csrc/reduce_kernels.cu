@@ -303,6 +303,145 @@ __global__ void k_projected_final(const double *__restrict__ part, int nslices, 
     out[(long)q * nslices + k] = v.s + v.c;
 }
 
+// ProjectedEnergyDensity.PoyntingComputation (diagnostics/methods/ProjectedEnergyDensity.java:182-279),
+// SU(2): per cell the averaged longitudinal Poynting vector (E averaged over
+// the link and its transported neighbour, F from the eight plaquettes of the
+// (dir, i) plane at U and Unext) and the time-averaged one (E x B with B
+// averaged over U and Unext).  Every cell counts, as in the reference.
+template <typename R>
+__device__ __forceinline__ Q2<R> link_o(const LinkPlanes<SU2<R>, R> &Up, const Lat &L, const int *x, int d, int o) {
+    // Grid.getLink: U_d(x) for o > 0, U_d(x - d)^dagger for o < 0
+    int y[3] = {x[0], x[1], x[2]};
+    if (o < 0) y[d] = y[d] == 0 ? L.n[d] - 1 : y[d] - 1;
+    const long s = ((long)y[0] * L.n[1] + y[1]) * L.n[2] + y[2];
+    const Q2<R> u = Up.load(d, s);
+    return o < 0 ? SU2<R>::adj(u) : u;
+}
+__device__ __forceinline__ void step_pos(const Lat &L, int *x, int d, int o) {
+    x[d] = o > 0 ? (x[d] == L.n[d] - 1 ? 0 : x[d] + 1) : (x[d] == 0 ? L.n[d] - 1 : x[d] - 1);
+}
+// Grid.getPlaquette(index, d1, d2, o1, o2): U1 U2 U3 U4 around x -> x+o1 d1 -> +o2 d2 -> -o1 d1
+template <typename R>
+__device__ __forceinline__ Q2<R> plaq_o(const LinkPlanes<SU2<R>, R> &Up, const Lat &L, const int *x, int d1, int d2,
+                                        int o1, int o2) {
+    int y[3] = {x[0], x[1], x[2]};
+    Q2<R> P = link_o(Up, L, y, d1, o1);
+    step_pos(L, y, d1, o1);
+    P = SU2<R>::mul(P, link_o(Up, L, y, d2, o2));
+    step_pos(L, y, d2, o2);
+    P = SU2<R>::mul(P, link_o(Up, L, y, d1, -o1));
+    step_pos(L, y, d1, -o1);
+    return SU2<R>::mul(P, link_o(Up, L, y, d2, -o2));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) k_projected_poynting(const R *__restrict__ U, const R *__restrict__ Unext,
+                                                                    const R *__restrict__ E, Lat L, int dir,
+                                                                    double *__restrict__ part) {
+    using G = SU2<R>;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
+    const AlgPlanes<3, R> Ep{const_cast<R *>(E), L.V};
+    const int k = blockIdx.x, nsplit = gridDim.y;
+    const int o1 = (dir + 1) % 3, o2 = (dir + 2) % 3;
+    const long nt = L.V / L.n[dir];
+    const double area = (double)L.V / (double)L.n[dir];
+    const double sa = sqrt(area);
+    KSum acc[2] = {{0, 0}, {0, 0}};
+    for (long t = (long)blockIdx.y * blockDim.x + threadIdx.x; t < nt; t += (long)nsplit * blockDim.x) {
+        int x[3];
+        x[dir] = k;
+        const int lo = (o1 > o2) ? o1 : o2, hi = (o1 > o2) ? o2 : o1;
+        x[lo] = (int)(t % L.n[lo]);
+        x[hi] = (int)(t / L.n[lo]);
+        const long s = x[0] * L.stride[0] + x[1] * L.stride[1] + x[2];
+        const Nbr nb = neighbours(L, s, x);
+        double lavg = 0.0;
+#pragma unroll 1
+        for (int i = 0; i < 3; i++) {
+            if (i == dir) continue;
+            Q2<R> FG = G::zero();
+#pragma unroll 1
+            for (int tt = 0; tt < 2; tt++) {
+                const LinkPlanes<G, R> &W = tt == 0 ? Up : Unp;
+                G::add(FG, plaq_o(W, L, x, dir, i, 1, 1));
+                G::add(FG, plaq_o(W, L, x, i, dir, -1, 1));
+                G::add(FG, plaq_o(W, L, x, i, dir, 1, -1));
+                G::add(FG, plaq_o(W, L, x, dir, i, -1, -1));
+            }
+            R F[3], e1[3], e2[3], e2t[3];
+            G::proj(FG, F);
+            const double ufF = 1.0 / ((L.a[i] * L.a[dir]) * L.g * sa);
+            const double ufEB = 1.0 / ((L.g * L.a[i]) * sa);
+            Ep.load_ro(i, s, e1);
+            Ep.load_ro(i, nb.bwd[i], e2);
+            G::act(e2, G::adj(Up.load(i, nb.bwd[i])), e2t);
+            double dot = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double fv = (double)F[c] * (ufF / 8.0);
+                const double ev = ((double)e1[c] + (double)e2t[c]) * (0.5 * ufEB);
+                dot += ev * fv;
+            }
+            lavg += dot;
+        }
+        const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
+        const double uf1 = 1.0 / ((L.g * L.a[d1]) * sa), uf2 = 1.0 / ((L.g * L.a[d2]) * sa);
+        R E1[3], E2[3], b10[3], b11[3], b20[3], b21[3];
+        Ep.load_ro(d1, s, E1);
+        Ep.load_ro(d2, s, E2);
+        field_b<G, R>(Up, L, s, nb, d1, b10);
+        field_b<G, R>(Unp, L, s, nb, d1, b11);
+        field_b<G, R>(Up, L, s, nb, d2, b20);
+        field_b<G, R>(Unp, L, s, nb, d2, b21);
+        double p12 = 0.0, p21 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const double B1 = ((double)b10[c] + (double)b11[c]) * (uf1 * 0.5);
+            const double B2 = ((double)b20[c] + (double)b21[c]) * (uf2 * 0.5);
+            p12 += ((double)E1[c] * uf1) * B2;
+            p21 += ((double)E2[c] * uf2) * B1;
+        }
+        two_sum_add(acc[0], lavg);
+        two_sum_add(acc[1], p12 - p21);
+    }
+    int q;
+    KSum v = block_reduce<2>(acc, q);
+    if (q >= 0) {
+        const long o = (((long)k * nsplit + blockIdx.y) * 2 + q) * 2;
+        part[o] = v.s;
+        part[o + 1] = v.c;
+    }
+}
+
+__global__ void k_poynting_final(const double *__restrict__ part, int nslices, int nsplit, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = q * nslices + k
+    if (i >= 2 * nslices) return;
+    const int q = i / nslices, k = i % nslices;
+    KSum v{0.0, 0.0};
+    for (int b = 0; b < nsplit; b++) {
+        const long o = (((long)k * nsplit + b) * 2 + q) * 2;
+        ksum_merge(v, KSum{part[o], part[o + 1]});
+    }
+    out[(long)q * nslices + k] = v.s + v.c;
+}
+
+int launch_projected_poynting(Ctx &c, int dir, double *out) {
+    if (c.nc != 2) return OPX_ERR_UNSUPPORTED;
+    const int ns = c.L.n[dir];
+    const long nt = c.L.V / ns;
+    int nsplit = (int)std::max<long>(1, std::min<long>(c.red_blocks / ns, nt / RED_THREADS));
+    nsplit = std::max(1, std::min(nsplit, (int)(c.red_blocks * 4 / ns)));  // 4 doubles per (slice, split)
+    if (c.prec == OPX_F64)
+        k_projected_poynting<double><<<dim3(ns, nsplit), RED_THREADS, 0, c.stream>>>(
+            (const double *)c.U, (const double *)c.Unext, (const double *)c.E, c.L, dir, c.red_part);
+    else
+        k_projected_poynting<float><<<dim3(ns, nsplit), RED_THREADS, 0, c.stream>>>(
+            (const float *)c.U, (const float *)c.Unext, (const float *)c.E, c.L, dir, c.red_part);
+    k_poynting_final<<<grid_for(2L * ns, 128), 128, 0, c.stream>>>(c.red_part, ns, nsplit, out);
+    c.launches += 2;
+    return OPX_OK;
+}
+
 template <int NC, typename R>
 __global__ void k_gauss_field(const R *__restrict__ U, const R *__restrict__ E, const R *__restrict__ rho, Lat L,
                               double *__restrict__ out) {

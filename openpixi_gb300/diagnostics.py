@@ -132,9 +132,8 @@ class ProjectedEnergyDensity(Diagnostics):
         self.direction = int(direction)
         self.computeEnergyDensity = compute_energy_density
         self.computePoyntingVector = compute_poynting_vector
-        if compute_poynting_vector:
-            raise NotImplementedError("ProjectedEnergyDensity: the Poynting vector rows are not provided")
         self.last = None
+        self.last_poynting = None
 
     def initialize(self, s):
         self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
@@ -144,12 +143,15 @@ class ProjectedEnergyDensity(Diagnostics):
         if steps % self.stepInterval != 0:
             return
         rows = grid.projected_energy(self.direction) if self.computeEnergyDensity else None
+        prow = grid.projected_poynting(self.direction) if self.computePoyntingVector else None
         self.last = rows
+        self.last_poynting = prow
         with open(self.path, "a") as f:
             f.write(java_double(steps * grid.getTemporalSpacing()) + "\n")
-            if rows is not None:
-                for r in rows:
-                    f.write("\t".join(java_sci(v) for v in r) + "\n")
+            for block in (rows, prow):
+                if block is not None:
+                    for r in block:
+                        f.write("\t".join(java_sci(v) for v in r) + "\n")
 
 
 class TimeMeasurement(Diagnostics):

@@ -201,6 +201,10 @@ class Grid:
     def projected_energy(self, d):
         return self.handle.projected_energy(d)
 
+    def projected_poynting(self, d):
+        """ProjectedEnergyDensity Poynting rows [2][N_d] (SU(2))."""
+        return self.handle.projected_poynting(d)
+
     def gauss_field(self):
         return self.handle.gauss_field()
 

@@ -177,6 +177,13 @@ class OracleGrid:
         lib().orc_gauss_constraint(self.pp, _p(self.U), _p(self.E), _p(self.rho), C.c_long(index), _p(out))
         return out
 
+    def projected_poynting(self, d):
+        out = np.empty(2 * self.dims[d])
+        rc = lib().orc_projected_poynting(self.pp, _p(self.U), _p(self.Unext), _p(self.E), d, _p(out))
+        if rc != 0:
+            raise ValueError("Poynting vector: SU(2) only")
+        return out.reshape(2, self.dims[d])
+
     def gauss_field(self):
         out = np.empty((self.V, na(self.nc)))
         lib().orc_gauss_field(self.pp, _p(self.U), _p(self.E), _p(self.rho), _p(out))

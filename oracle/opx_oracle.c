@@ -705,6 +705,75 @@ void orc_projected_energy(const orc_params *p, const double *U, const double *Un
     }
 }
 
+/* ProjectedEnergyDensity.PoyntingComputation (diagnostics/methods/ProjectedEnergyDensity.java:182-279),
+ * SU(2) only (SU3AlgebraElement.mult(AlgebraElement) throws in the reference).
+ * Every cell counts (the computation has no isEvaluatable test).
+ * out: 2 rows of N[dir]: Poynting vector averaged, and only time-averaged. */
+int orc_projected_poynting(const orc_params *p, const double *U, const double *Unext,
+                           const double *E, int dir, double *out)
+{
+    if (p->nc != 2) return -1;
+    const int na = 3, ng = 4;
+    long V = vol(p);
+    int N = p->n[dir];
+    double *avg = out, *tavg = out + N;
+    for (int i = 0; i < 2 * N; i++) out[i] = 0.0;
+    double areaFactor = V / ((double)N);
+    double ufF[3], ufEB[3];
+    for (int i = 0; i < 3; i++) {
+        ufF[i] = 1.0 / ((p->a[i] * p->a[dir]) * p->g * sqrt(areaFactor));
+        ufEB[i] = 1.0 / ((p->g * p->a[i]) * sqrt(areaFactor));
+    }
+    const int d = dir;
+    for (long x = 0; x < V; x++) {
+        double lavg = 0.0, ltavg = 0.0;
+        for (int i = 0; i < 3; i++) {
+            if (i == d) continue;
+            double FG[NG_MAX] = {0}, P[NG_MAX];
+            for (int t = 0; t < 2; t++) {
+                const double *W = t ? Unext : U;
+                orc_plaquette(p, W, x, d, i, 1, 1, P);
+                for (int c = 0; c < ng; c++) FG[c] += P[c];
+                orc_plaquette(p, W, x, i, d, -1, 1, P);
+                for (int c = 0; c < ng; c++) FG[c] += P[c];
+                orc_plaquette(p, W, x, i, d, 1, -1, P);
+                for (int c = 0; c < ng; c++) FG[c] += P[c];
+                orc_plaquette(p, W, x, d, i, -1, -1, P);
+                for (int c = 0; c < ng; c++) FG[c] += P[c];
+            }
+            double F[NA_MAX], E1[NA_MAX], E2[NA_MAX], g[NG_MAX], Ev[NA_MAX];
+            orc_group_proj(2, FG, F);
+            for (int c = 0; c < na; c++) F[c] = F[c] * (ufF[i] / 8.0);
+            long sh = orc_shift(p, x, i, -1);
+            memcpy(E1, E + ((size_t)x * 3 + i) * na, sizeof(double) * na);
+            get_link(p, U, x, i, -1, g);
+            orc_alg_act(2, E + ((size_t)sh * 3 + i) * na, g, E2);
+            for (int c = 0; c < na; c++) Ev[c] = (E1[c] + E2[c]) * (0.5 * ufEB[i]);
+            lavg += Ev[0] * F[0] + Ev[1] * F[1] + Ev[2] * F[2];
+        }
+        int dir1 = (d + 1) % 3, dir2 = (d + 2) % 3;
+        double e1[NA_MAX], e2[NA_MAX], b10[NA_MAX], b11[NA_MAX], b20[NA_MAX], b21[NA_MAX], B1[NA_MAX], B2[NA_MAX];
+        for (int c = 0; c < na; c++) {
+            e1[c] = E[((size_t)x * 3 + dir1) * na + c] * ufEB[dir1];
+            e2[c] = E[((size_t)x * 3 + dir2) * na + c] * ufEB[dir2];
+        }
+        orc_get_b(p, U, x, dir1, b10);
+        orc_get_b(p, Unext, x, dir1, b11);
+        orc_get_b(p, U, x, dir2, b20);
+        orc_get_b(p, Unext, x, dir2, b21);
+        for (int c = 0; c < na; c++) {
+            B1[c] = (b10[c] + b11[c]) * (ufEB[dir1] * 0.5);
+            B2[c] = (b20[c] + b21[c]) * (ufEB[dir2] * 0.5);
+        }
+        ltavg = (e1[0] * B2[0] + e1[1] * B2[1] + e1[2] * B2[2]) - (e2[0] * B1[0] + e2[1] * B1[1] + e2[2] * B1[2]);
+        int pos[3];
+        cell_pos(p, x, pos);
+        avg[pos[d]] += lavg;
+        tavg[pos[d]] += ltavg;
+    }
+    return 0;
+}
+
 void orc_gauss_field(const orc_params *p, const double *U, const double *E, const double *rho,
                      double *out)
 {

@@ -100,6 +100,9 @@ void orc_energy_density(const orc_params *p, const double *U, const double *Unex
 /* out: 4 rows of N[dir]: T_el, T_mag, L_el, L_mag (ProjectedEnergyDensity order) */
 void orc_projected_energy(const orc_params *p, const double *U, const double *Unext,
                           const double *E, const uint8_t *eval, int dir, double *out);
+/* out: 2 rows of N[dir]: Poynting averaged, time-averaged (SU(2); -1 for SU(3)) */
+int orc_projected_poynting(const orc_params *p, const double *U, const double *Unext,
+                           const double *E, int dir, double *out);
 void orc_gauss_field(const orc_params *p, const double *U, const double *E,
                      const double *rho, double *out /* [V][na] */);
 

@@ -258,3 +258,24 @@ def test_fp32_su3_pair_reduction(native, orc, dims):
         h.step(3)
     a, b = bulk_vec(hp.reduce()), bulk_vec(hs.reduce())
     assert np.all(np.abs(a - b) <= 1e-6 * np.abs(b) + 1e-12), (a, b)
+
+
+def test_projected_poynting_matches_oracle(native, orc):
+    """ProjectedEnergyDensity Poynting rows (SU(2)) against the oracle on a
+    lattice with uneven spacings, every direction: 1e-12 of the largest
+    row value; SU(3) handles report OPX_ERR_UNSUPPORTED (the reference throws)."""
+    g = fresh(oracle_ic(2, (8, 6, 10), 31, 0.4, 0.3, dt=0.1, a=(1.0, 0.9, 1.2)))
+    h = handle_from_oracle(g)
+    sim = orc.OracleSimulation(g)
+    sim.initialize()
+    h.initialize()
+    for _ in range(3):
+        sim.step()
+        h.step(1)
+    for d in range(3):
+        ref = g.projected_poynting(d)
+        got = h.projected_poynting(d)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), d
+    h3 = opx.Handle(3, (4, 4, 4))
+    with pytest.raises(opx.OpixiError):
+        h3.projected_poynting(0)

@@ -244,3 +244,93 @@ def test_ngp_rounds_half_even(orc):
     pos = np.array([[0.5, 1.5, 2.5], [2.4999, -0.5, 7.5000001]])
     c = P.ngp(g, pos)
     assert c.tolist() == [[0, 2, 2], [2, 0, 8]]
+
+
+# ---------------------------------------------------------------- Poynting rows
+def _su2_mat(q):
+    """quaternion (e0, e1, e2, e3) -> e0 + i e.sigma as a 2x2 complex matrix"""
+    e0, e1, e2, e3 = q
+    return np.array([[e0 + 1j * e3, e2 + 1j * e1], [-e2 + 1j * e1, e0 - 1j * e3]])
+
+
+def _su2_proj(M):
+    """2 (e1, e2, e3) of a real-linear combination of SU(2) matrices"""
+    return 2.0 * np.array([M[0, 1].imag, M[0, 1].real, M[0, 0].imag])
+
+
+_SIG = [np.array([[0, 1], [1, 0]], complex), np.array([[0, -1j], [1j, 0]]), np.array([[1, 0], [0, -1]], complex)]
+
+
+def _alg_mat(v):
+    return sum(v[a] * _SIG[a] for a in range(3)) / 2.0
+
+
+def _alg_vec(X):
+    return np.array([np.trace(_SIG[a] @ X).real for a in range(3)])
+
+
+def test_poynting_rows_against_independent_matrices(orc):
+    """ProjectedEnergyDensity.PoyntingComputation (ProjectedEnergyDensity.java:182-279)
+    restated a second time with numpy 2x2 matrices on a small uneven SU(2) lattice."""
+    dims, a, g_, dt = (4, 3, 5), (1.0, 0.9, 1.2), 1.3, 0.1
+    g = orc.OracleGrid(2, dims, a=a, dt=dt, g=g_)
+    g.random_links(3, 0.7)
+    g.random_e(3, 0.5)
+    g.update_links()
+    # the independent 2x2 form must agree with the oracle's act first
+    X = _alg_mat(g.E[7, 1])
+    Um = _su2_mat(g.U[5, 2])
+    assert np.allclose(_alg_vec(Um @ X @ Um.conj().T), orc.alg_act(2, g.E[7, 1], g.U[5, 2]), atol=1e-13)
+    V = g.V
+
+    def idx(p):
+        return ((p[0] % dims[0]) * dims[1] + (p[1] % dims[1])) * dims[2] + (p[2] % dims[2])
+
+    def link(W, p, d, o):
+        if o > 0:
+            return _su2_mat(W[idx(p), d])
+        q = list(p); q[d] -= 1
+        return _su2_mat(W[idx(q), d]).conj().T
+
+    def plaq(W, p, d1, d2, o1, o2):
+        x1 = list(p)
+        x2 = list(x1); x2[d1] += o1
+        x3 = list(x2); x3[d2] += o2
+        x4 = list(x3); x4[d1] -= o1
+        return link(W, x1, d1, o1) @ link(W, x2, d2, o2) @ link(W, x3, d1, -o1) @ link(W, x4, d2, -o2)
+
+    for d in range(3):
+        N = dims[d]
+        area = V / N
+        ufF = [1.0 / ((a[i] * a[d]) * g_ * np.sqrt(area)) for i in range(3)]
+        ufEB = [1.0 / ((g_ * a[i]) * np.sqrt(area)) for i in range(3)]
+        avg, tavg = np.zeros(N), np.zeros(N)
+        for x in range(V):
+            p = [x // (dims[1] * dims[2]), (x // dims[2]) % dims[1], x % dims[2]]
+            la = 0.0
+            for i in range(3):
+                if i == d:
+                    continue
+                FG = np.zeros((2, 2), complex)
+                for W in (g.U, g.Unext):
+                    FG += plaq(W, p, d, i, 1, 1) + plaq(W, p, i, d, -1, 1) + plaq(W, p, i, d, 1, -1) \
+                        + plaq(W, p, d, i, -1, -1)
+                F = _su2_proj(FG) * ufF[i] / 8.0
+                q = list(p); q[i] -= 1
+                Ub = link(g.U, p, i, -1)
+                E2 = _alg_vec(Ub @ _alg_mat(g.E[idx(q), i]) @ Ub.conj().T)
+                la += np.dot((g.E[x, i] + E2) * 0.5 * ufEB[i], F)
+            d1, d2 = (d + 1) % 3, (d + 2) % 3
+
+            def bvec(W, dd):
+                j, k = (dd + 1) % 3, (dd + 2) % 3
+                return _su2_proj(plaq(W, p, j, k, 1, 1)) * a[dd] / (a[j] * a[k])
+            B1 = (bvec(g.U, d1) + bvec(g.Unext, d1)) * ufEB[d1] * 0.5
+            B2 = (bvec(g.U, d2) + bvec(g.Unext, d2)) * ufEB[d2] * 0.5
+            ta = np.dot(g.E[x, d1] * ufEB[d1], B2) - np.dot(g.E[x, d2] * ufEB[d2], B1)
+            avg[p[d]] += la
+            tavg[p[d]] += ta
+        ref = np.stack([avg, tavg])
+        got = g.projected_poynting(d)
+        assert np.allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max()), (d, got, ref)
+        assert np.abs(ref).max() > 1e-4
