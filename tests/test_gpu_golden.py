@@ -44,7 +44,8 @@ def test_leapfrog_golden(native, name):
         got = np.array(list(o.e2) + list(o.b2) + [o.px, o.py, o.pz, o.gauss, o.rho2, o.e2_total, o.b2_total])
         ref = f["bulk"][k]
         assert np.all(np.abs(got[:6] - ref[:6]) <= 1e-12 * np.abs(ref[:6]) + 1e-300), k
-        assert abs(got[9] - ref[9]) <= 1e-12 * max(abs(ref[9]), 1e-20), k
+        # the Gauss column sits at rounding level (mean G^2 ~ 1e-30): absolute bar
+        assert abs(got[9] - ref[9]) <= 1e-12 * abs(ref[9]) + 1e-26, k
     assert link_rel_err(h.download(N.FIELD_U), f["U"]) <= 1e-10
     assert link_rel_err(h.download(N.FIELD_UNEXT), f["Unext"]) <= 1e-10
     assert field_rel_err(h.download(N.FIELD_E), f["E"]) <= 1e-10
