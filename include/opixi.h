@@ -265,8 +265,9 @@ long opx_batch_kernel_launches(const opx_batch *b);
  * synchronisation of cudaMalloc/cudaFree.  Computes what opx_reduce computes
  * and writes one opx_observables record to out_device (device memory), queued
  * on `stream` (a cudaStream_t; NULL = the default stream).  Fields are device
- * pointers in the handle's layout: links U, Unext in warp-sized site blocks
- * [3][ceil(V/32)][ng][32], algebra fields as planes E [3][ngen][V],
+ * pointers in the handle's layout: SU(3) links U, Unext in warp-sized site
+ * blocks [3][ceil(V/32)][18][32], SU(2) links as [3][32 ceil(V/32)][4]
+ * (quaternion components contiguous), algebra fields as planes E [3][ngen][V],
  * rho [ngen][V] (NULL = zero charge), eval [V] (NULL = all cells), elements
  * double (OPX_F64) or float (OPX_F32).
  * Calls no cudaMalloc/cudaFree: its scratch is a fixed 77,824-byte __device__

@@ -184,9 +184,8 @@ __global__ void k_adj_gather(const double *__restrict__ Wprev, const double *__r
 }
 
 __device__ __forceinline__ void atomic_add_link(double *base, long V, int d, long s, const Q &q) {
-    double *b = base + link_offset(V, 4, d, 0, s);
 #pragma unroll
-    for (int k = 0; k < 4; k++) atomicAdd(b + 32 * k, q.e[k]);
+    for (int k = 0; k < 4; k++) atomicAdd(base + link_offset(V, 4, d, k, s), q.e[k]);
 }
 
 __device__ __forceinline__ bool in_box(const int *x, const int *lo, const int *hi) {

@@ -51,7 +51,8 @@ template <typename R>
 __global__ void k_fill_identity(R *U, long V, int ng, int nc) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over the blocked link array
     if (t >= link_elems(V, ng)) return;
-    const int c = (int)((t >> 5) % ng);
+    // component index of element t in the link layout (lattice.cuh)
+    const int c = ng == 4 ? (int)(t & 3) : (int)((t >> 5) % ng);
     const bool one = nc == 3 ? (c == 0 || c == 4 || c == 8) : (c == 0);
     U[t] = one ? R(1) : R(0);
 }

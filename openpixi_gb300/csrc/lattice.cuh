@@ -136,9 +136,13 @@ template <typename R> __device__ __forceinline__ R ld(const R *p) { return *p; }
 template <> __device__ __forceinline__ float ld<float>(const float *p) { return __ldg(p); }
 template <> __device__ __forceinline__ double ld<double>(const double *p) { return __ldg(p); }
 
-// Warp-blocked link layout
+// Link layouts.  SU(3) (NG = 18): warp-blocked, component c of 32 consecutive
+// sites contiguous.  SU(2) (NG = 4): the four quaternion components of a link
+// contiguous (one 16-byte vector load in FP32, two in FP64), links of
+// consecutive sites consecutive.  Both pad the site count to a multiple of 32.
 __host__ __device__ __forceinline__ long link_blocks(long V) { return (V + 31) >> 5; }
 __host__ __device__ __forceinline__ long link_offset(long V, int NG, int d, int c, long s) {
+    if (NG == 4) return ((long)d * (link_blocks(V) << 5) + s) * 4 + c;
     return (((long)d * link_blocks(V) + (s >> 5)) * NG + c) * 32 + (s & 31);
 }
 __host__ __device__ __forceinline__ long link_elems(long V, int NG) { return 3L * link_blocks(V) * 32 * NG; }
@@ -151,16 +155,40 @@ template <class G, typename R> struct LinkPlanes {
     __device__ __forceinline__ void store(int d, long s, const typename G::M &m) const;
 };
 
+// Four contiguous reals: vector loads and stores for the built-in types.
+template <typename R> __device__ __forceinline__ void ld4(const R *b, R *e) {
+    e[0] = b[0]; e[1] = b[1]; e[2] = b[2]; e[3] = b[3];
+}
+template <> __device__ __forceinline__ void ld4<float>(const float *b, float *e) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(b));
+    e[0] = v.x; e[1] = v.y; e[2] = v.z; e[3] = v.w;
+}
+template <> __device__ __forceinline__ void ld4<double>(const double *b, double *e) {
+    const double2 v0 = __ldg(reinterpret_cast<const double2 *>(b));
+    const double2 v1 = __ldg(reinterpret_cast<const double2 *>(b) + 1);
+    e[0] = v0.x; e[1] = v0.y; e[2] = v1.x; e[3] = v1.y;
+}
+template <typename R> __device__ __forceinline__ void st4(R *b, const R *e) {
+    b[0] = e[0]; b[1] = e[1]; b[2] = e[2]; b[3] = e[3];
+}
+template <> __device__ __forceinline__ void st4<float>(float *b, const float *e) {
+    *reinterpret_cast<float4 *>(b) = make_float4(e[0], e[1], e[2], e[3]);
+}
+template <> __device__ __forceinline__ void st4<double>(double *b, const double *e) {
+    reinterpret_cast<double2 *>(b)[0] = make_double2(e[0], e[1]);
+    reinterpret_cast<double2 *>(b)[1] = make_double2(e[2], e[3]);
+}
+
 template <typename R> struct LinkPlanes<SU2<R>, R> {
     R *p;
     long V;
     __device__ __forceinline__ Q2<R> load(int d, long s) const {
-        const R *b = p + link_offset(V, 4, d, 0, s);
-        return Q2<R>{{ld(b), ld(b + 32), ld(b + 64), ld(b + 96)}};
+        Q2<R> q;
+        ld4<R>(p + link_offset(V, 4, d, 0, s), q.e);
+        return q;
     }
     __device__ __forceinline__ void store(int d, long s, const Q2<R> &m) const {
-        R *b = p + link_offset(V, 4, d, 0, s);
-        b[0] = m.e[0]; b[32] = m.e[1]; b[64] = m.e[2]; b[96] = m.e[3];
+        st4<R>(p + link_offset(V, 4, d, 0, s), m.e);
     }
 };
 
