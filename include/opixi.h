@@ -163,7 +163,8 @@ int opx_particles_download(opx_ctx *ctx, opx_particles *p);
 long opx_particles_count(const opx_ctx *ctx);
 /* Particle phases of one Simulation.step (reassign != 0) or of
  * Simulation.initialize (reassign == 0): charge density, positions, transport,
- * charges, currents (Simulation.java:398-421, 329-347). */
+ * charges, currents (Simulation.java:398-421, 329-347).  With super particles:
+ * their charge density and current at the handle's step count. */
 int opx_cpic_phases(opx_ctx *ctx, int reassign);
 
 /* ---- CGC initial conditions (physics/initial/CGC/CGCInitialCondition.java:55-93) ----
@@ -190,6 +191,26 @@ typedef struct {
  * Simulation.initialize.  use_seed == 0 draws an unseeded stream.  OPX_F64
  * handles, beam along direction 0.  Call opx_initialize afterwards. */
 int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
+
+/* ---- super particles: simulationType "temporal optimized cgc ngp"
+ *      (Settings.java:566-571: CGCSuperParticleSolver + CGCSuperParticleInterpolationNGP;
+ *      physics/particles/CGCSuperParticle.java) ----
+ * The nuclei's particles are created by LightConeNGPSuperParticleCreator
+ * (physics/initial/CGC/LightConeNGPSuperParticleCreator.java:102-241): per nucleus
+ * a group of round(aL/dt) super particles k, each a block of charges over the
+ * particle block [base, base + n) of global cell indices, moving along
+ * direction 0.  opx_initialize / opx_step then run the charge density and
+ * current of CGCSuperParticleInterpolationNGP (:19-93) instead of the NGP
+ * particle phases.  OPX_F64 handles, beam along direction 0; a handle holds
+ * either NGP particles or super particles. */
+int opx_cgc_mv_super(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
+/* number of super-particle groups on the handle */
+int opx_super_groups(const opx_ctx *ctx);
+/* group g: orientation, n, base and (Q != NULL) the charges Q[k][i][na_ref]
+ * (reference layout; count = round(aL/dt) * n * na_ref) */
+int opx_super_download(opx_ctx *ctx, int group, int *orientation, long *n, long *base, double *Q, size_t count);
+/* appends a group with charges Q[k][i][na_ref] (the layout of opx_super_download) */
+int opx_super_upload(opx_ctx *ctx, int orientation, long n, long base, const double *Q);
 
 /* ---- seeded synthetic initial conditions (no counterpart in the reference) ---- */
 /* U_i(x) = exp(i A_i^a(x) t_a), A ~ N(0, sigma_a^2); E_i^a(x) ~ N(0, sigma_e^2);

@@ -42,7 +42,8 @@ EXPORTED = [
     "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
     "opx_batch_kernel_launches",
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
-    "opx_particles_count", "opx_projected_poynting",
+    "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
+    "opx_super_download", "opx_super_upload",
 ]
 
 
@@ -143,6 +144,10 @@ def load(path=None):
         "opx_cgc_mv": (C.c_int, [vp, vp, C.c_int]),
         "opx_particles_count": (C.c_long, [vp]),
         "opx_projected_poynting": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
+        "opx_cgc_mv_super": (C.c_int, [vp, vp, C.c_int]),
+        "opx_super_groups": (C.c_int, [vp]),
+        "opx_super_download": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, C.c_size_t]),
+        "opx_super_upload": (C.c_int, [vp, C.c_int, C.c_long, C.c_long, vp]),
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
         "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
@@ -180,6 +185,8 @@ class Handle:
             raise OpixiError(rc, self.L.opx_last_error(None).decode())
         self.h = h
         self.ncolors = int(ncolors)
+        self.a = tuple(float(x) for x in a)
+        self.dt = float(dt)
         self.dims = tuple(int(d) for d in dims)
         self.V = int(np.prod(self.dims))
         self.precision = precision
@@ -326,6 +333,30 @@ class Handle:
                 setattr(arr[k], f, nu[f])
         self.check(self.L.opx_cgc_mv(self.h, arr, len(nuclei)))
         self.np = self.L.opx_particles_count(self.h)
+
+    # ---- super particles (temporal optimized cgc ngp) ----
+    def cgc_mv_super(self, nuclei):
+        arr = (MVNucleus * len(nuclei))()
+        for k, nu in enumerate(nuclei):
+            for f, _ in MVNucleus._fields_:
+                setattr(arr[k], f, nu[f])
+        self.check(self.L.opx_cgc_mv_super(self.h, arr, len(nuclei)))
+
+    @property
+    def super_groups(self):
+        return self.L.opx_super_groups(self.h)
+
+    def super_download(self, g):
+        o, n, b = C.c_int(), C.c_long(), C.c_long()
+        self.check(self.L.opx_super_download(self.h, int(g), C.byref(o), C.byref(n), C.byref(b), None, 0))
+        ppc = int(round(self.a[0] / self.dt))
+        Q = np.empty((ppc, n.value, self.na_ref))
+        self.check(self.L.opx_super_download(self.h, int(g), None, None, None, ptr(Q), Q.size))
+        return {"orientation": o.value, "n": n.value, "base": b.value, "Q": Q}
+
+    def super_upload(self, orientation, n, base, Q):
+        q = np.ascontiguousarray(Q, dtype=np.float64)
+        self.check(self.L.opx_super_upload(self.h, int(orientation), int(n), int(base), ptr(q) if q.size else None))
 
     # ---- differentiation form (SU(2)) ----
     @staticmethod

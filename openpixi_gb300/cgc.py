@@ -64,13 +64,20 @@ class CGCInitialCondition:
         self.poissonSolver = "improved"
 
     def applyInitialCondition(self, s):
-        if s.simulationType != "TemporalCGCNGP":
+        # the particle creator follows the simulation type (CGCInitialCondition.java:76-87)
+        if s.simulationType not in ("TemporalCGCNGP", "TemporalOptimizedCGCNGP"):
             raise RuntimeError("CGCInitialCondition: simulation type not supported!")
         if self.computeTadpole or self.computeDipole:
             raise NotImplementedError("Wilson line observables (tadpole, dipole) are not provided")
         h = s.grid.handle
-        h.cgc_mv([self.initialChargeDensity.as_nucleus()])
-        s.particles = h.np
+        if s.simulationType == "TemporalOptimizedCGCNGP":
+            # LightConeNGPSuperParticleCreator: CGCSuperParticle groups
+            h.cgc_mv_super([self.initialChargeDensity.as_nucleus()])
+            s.particles = h.super_groups
+        else:
+            # LightConeNGPParticleCreator: CGCParticle list
+            h.cgc_mv([self.initialChargeDensity.as_nucleus()])
+            s.particles = h.np
         s.grid._dirty()
 
     @staticmethod

@@ -66,6 +66,7 @@ static void fill_identity(Ctx &c, void *U) {
 
 static void release(Ctx &c) {
     cpic_free(c);
+    super_free(c);
     void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.status};
     for (void *p : dev) if (p) cudaFree(p);
     if (c.red_host) cudaFreeHost(c.red_host);
@@ -321,7 +322,8 @@ int opx_cpic_phases(opx_ctx *ctx, int reassign) {
     int rc = cpic_ok(c, "opx_cpic_phases");
     if (rc) return rc;
     phase_begin(c);
-    launch_cpic_phases(c, reassign);
+    if (!c.sg.empty()) launch_super_phases(c, c.steps);  // the step counter is the simulation step t
+    else launch_cpic_phases(c, reassign);
     phase_end(c, OPX_PHASE_CPIC);
     return check_launch(c, "opx_cpic_phases");
 }
@@ -332,6 +334,10 @@ int opx_initialize(opx_ctx *ctx) {
     int rc = opx_step_links(ctx);
     if (rc) return rc;
     if (c.P.n > 0) return opx_cpic_phases(ctx, 0);
+    if (!c.sg.empty()) {
+        launch_super_phases(c, c.steps);
+        return check_launch(c, "opx_initialize");
+    }
     return OPX_OK;
 }
 
@@ -345,6 +351,10 @@ static int one_step(Ctx &c) {
     if (c.P.n > 0) {
         phase_begin(c);
         launch_cpic_phases(c, 1);
+        phase_end(c, OPX_PHASE_CPIC);
+    } else if (!c.sg.empty()) {
+        phase_begin(c);
+        launch_super_phases(c, c.steps);
         phase_end(c, OPX_PHASE_CPIC);
     }
     return OPX_OK;
@@ -454,6 +464,7 @@ int opx_particles_upload(opx_ctx *ctx, const opx_particles *p) {
     int rc = cpic_ok(c, "opx_particles_upload");
     if (rc) return rc;
     if (!p || p->n < 0) { c.err = "opx_particles_upload: invalid particle list"; return OPX_ERR_INVALID; }
+    if (!c.sg.empty()) { c.err = "opx_particles_upload: the handle holds super particles"; return OPX_ERR_INVALID; }
     const long n = p->n;
     if (n > 0 && (!p->pos0 || !p->pos1 || !p->vel || !p->Q0 || !p->Q1 || !p->dir)) {
         c.err = "opx_particles_upload: null array";
@@ -526,6 +537,67 @@ int opx_particles_download(opx_ctx *ctx, opx_particles *p) {
 }
 
 long opx_particles_count(const opx_ctx *ctx) { return ctx ? ctx->c.P.n : -1; }
+
+int opx_super_groups(const opx_ctx *ctx) { return ctx ? (int)ctx->c.sg.size() : -1; }
+
+int opx_super_download(opx_ctx *ctx, int group, int *orientation, long *n, long *base, double *Q, size_t count) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (group < 0 || group >= (int)c.sg.size()) { c.err = "opx_super_download: no such group"; return OPX_ERR_INVALID; }
+    const SuperGroup &G = c.sg[group];
+    if (orientation) *orientation = G.orientation;
+    if (n) *n = G.n;
+    if (base) *base = G.base;
+    if (!Q) return OPX_OK;
+    const int nar = c.na_ref, ppc = c.sg_ppc;
+    const size_t tot = (size_t)ppc * G.n * nar;
+    if (count != tot) { c.err = "opx_super_download: Q must hold ppc*n*na_ref doubles"; return OPX_ERR_INVALID; }
+    int rc = sync_check(c, "opx_super_download");
+    if (rc) return rc;
+    std::vector<double> t(tot);
+    cudaError_t e = tot ? cudaMemcpy(t.data(), G.Q, sizeof(double) * tot, cudaMemcpyDeviceToHost) : cudaSuccess;
+    if (e != cudaSuccess) return cuda_fail(c, "opx_super_download", e);
+    // device [k][a][n] -> host [k][n][a]
+    for (int k = 0; k < ppc; k++)
+        for (long i = 0; i < G.n; i++)
+            for (int a = 0; a < nar; a++) Q[((size_t)k * G.n + i) * nar + a] = t[((size_t)k * nar + a) * G.n + i];
+    return OPX_OK;
+}
+
+int opx_super_upload(opx_ctx *ctx, int orientation, long n, long base, const double *Q) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (c.prec != OPX_F64) { c.err = "opx_super_upload: super particles require an OPX_F64 handle"; return OPX_ERR_UNSUPPORTED; }
+    if (c.P.n > 0) { c.err = "opx_super_upload: the handle holds NGP particles"; return OPX_ERR_INVALID; }
+    const int ppc = (int)std::lround(c.L.a[0] / c.L.dt);
+    if ((orientation != 1 && orientation != -1) || n < 0 || (n > 0 && !Q) || ppc < 1 ||
+        (int)(c.sg.size() + 1) * ppc > 64) {
+        c.err = "opx_super_upload: orientation +-1, n >= 0, round(a0/dt) >= 1, groups x round(a0/dt) <= 64";
+        return OPX_ERR_INVALID;
+    }
+    SuperGroup G;
+    G.orientation = orientation;
+    G.n = n;
+    G.base = base;
+    const int nar = c.na_ref;
+    const size_t tot = (size_t)ppc * n * nar;
+    if (tot) {
+        if (cudaMalloc(&G.Q, sizeof(double) * tot) != cudaSuccess) {
+            cudaGetLastError();
+            c.err = "opx_super_upload: out of device memory";
+            return OPX_ERR_NOMEM;
+        }
+        std::vector<double> t(tot);
+        for (int k = 0; k < ppc; k++)
+            for (long i = 0; i < n; i++)
+                for (int a = 0; a < nar; a++) t[((size_t)k * nar + a) * n + i] = Q[((size_t)k * n + i) * nar + a];
+        cudaError_t e = cudaMemcpy(G.Q, t.data(), sizeof(double) * tot, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { cudaFree(G.Q); return cuda_fail(c, "opx_super_upload", e); }
+    }
+    c.sg.push_back(G);
+    c.sg_ppc = ppc;
+    return OPX_OK;
+}
 
 int opx_init_random(opx_ctx *ctx, uint64_t seed, double sigma_a, double sigma_e) {
     API_CHECK(ctx);

@@ -362,6 +362,82 @@ __global__ void k_cgc_refine(double *__restrict__ q, int nar, long np, long ntr,
         }
 }
 
+// LightConeNGPSuperParticleCreator.initializeParticles (:150-199): charge i of
+// super particle k is G(ngp)/ppc with ngp = index (k < ppc/2) or index + one
+// plane, index = base + i; stored as Q[k][a][i] in the reference layout.
+template <int NC>
+__global__ void k_super_init(const double *__restrict__ Gv, long V, long ntr, long base, long n, int ppc,
+                             double *__restrict__ Q) {
+    constexpr int NA = NC == 3 ? 8 : 3;
+    constexpr int NAR = NC == 3 ? 9 : 3;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long index = base + i;
+    for (int k = 0; k < ppc; k++) {
+        const long ngp = (k < ppc / 2) ? index : (index + ntr >= V ? index + ntr - V : index + ntr);
+        double gen[NA], ref[NAR];
+        for (int a = 0; a < NA; a++) gen[a] = Gv[(long)a * V + ngp];
+        if (NC == 3) {
+            const double s3 = 1.7320508075688772;
+            for (int a = 0; a < NAR; a++) ref[a] = 0.0;
+            ref[1] += gen[0] / 2;
+            ref[3] += gen[1] / 2;
+            { const double dd = gen[2] / 2; ref[0] += dd; ref[4] -= dd; }
+            ref[2] += gen[3] / 2;
+            ref[6] += gen[4] / 2;
+            ref[5] += gen[5] / 2;
+            ref[7] += gen[6] / 2;
+            { const double cur = (ref[0] + ref[4] - 2 * ref[8]) / s3; const double dd = (gen[NA - 1] - cur) / 2;
+              ref[0] += dd / s3; ref[4] += dd / s3; ref[8] -= 2 * dd / s3; }
+        } else {
+            for (int a = 0; a < NAR; a++) ref[a] = gen[a];
+        }
+        for (int a = 0; a < NAR; a++) Q[((long)k * NAR + a) * n + i] = ref[a] * (1.0 / ppc);
+    }
+}
+
+// refine2 / refine4 (:200-302) on each transverse column's list: entry ii is
+// charge (ii / ppc) * ntr + t of super particle ii % ppc; the sweeps skip
+// entries with (ii + ppc/2) % ppc == ppc - 1.
+__global__ void k_super_refine(double *__restrict__ Q, int nar, long n, long ntr, int ppc, long len) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntr || len <= 0) return;
+    auto P = [&](long i, int a) -> double & {
+        const long ii = ((i % len) + len) % len;
+        return Q[((long)(ii % ppc) * nar + a) * n + (ii / ppc) * ntr + t];
+    };
+    for (int it = 0; it < 100; it++)
+        for (long i = 0; i < len; i++) {
+            const long jm = (i + ppc / 2) % ppc;
+            if (!(jm >= 0 && jm < ppc - 1)) continue;
+            for (int a = 0; a < nar; a++) {
+                double DQ = P(i - 1, a) * -1;
+                DQ += P(i, a) * 3;
+                DQ += P(i + 1, a) * -3;
+                DQ += P(i + 2, a) * 1;
+                DQ *= 1.0 / 4.0;
+                P(i, a) += DQ * -1.0;
+                P(i + 1, a) += DQ * 1.0;
+            }
+        }
+    for (int it = 0; it < 100; it++)
+        for (long i = 0; i < len; i++) {
+            const long jm = (i + ppc / 2) % ppc;
+            if (!(jm >= 0 && jm < ppc - 1)) continue;
+            for (int a = 0; a < nar; a++) {
+                double DQ = P(i - 2, a) * 1;
+                DQ += P(i - 1, a) * -5;
+                DQ += P(i, a) * 10;
+                DQ += P(i + 1, a) * -10;
+                DQ += P(i + 2, a) * 5;
+                DQ += P(i + 3, a) * -1;
+                DQ *= 1.0 / 12.0;
+                P(i, a) += DQ * -1.0;
+                P(i + 1, a) += DQ * 1.0;
+            }
+        }
+}
+
 }  // namespace opx
 
 using namespace opx;
@@ -378,7 +454,8 @@ struct Plan {
 
 // Host driver; returns the particles created for this nucleus (reference layout, host).
 static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &ppos0, std::vector<double> &ppos1,
-                       std::vector<double> &pvel, std::vector<double> &pq, std::vector<int32_t> &pdir) {
+                       std::vector<double> &pvel, std::vector<double> &pq, std::vector<int32_t> &pdir,
+                       SuperGroup *sg) {
     const int n0 = c.L.n[0], n1 = c.L.n[1], n2 = c.L.n[2];
     const long V = c.L.V, ntr = (long)n1 * n2;
     const int NA = c.na, nc = c.nc;
@@ -484,8 +561,40 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
         cudaError_t e = cudaStreamSynchronize(c.stream);
         if (e != cudaSuccess) { c.err = std::string("opx_cgc_mv: ") + cudaGetErrorString(e); rc = OPX_ERR_CUDA; }
     }
+    // 4b. super particles (LightConeNGPSuperParticleCreator.initializeParticles, :102-241)
+    if (!rc && sg) {
+        const int ppc = (int)std::lround(aL / c.L.dt);
+        double gmax = 0.0;
+        for (int z = 0; z < n0; z++) gmax = std::max(gmax, mx[z]);
+        const double cutoff = gmax * 10E-10;
+        int zStart = 0, zEnd = n0 - 1;
+        for (int z = 0; z < n0; z++) if (mx[z] > cutoff) { zStart = z; break; }
+        for (int z = zEnd - 1; z >= 0; z--) if (mx[z] > cutoff) { zEnd = z; break; }
+        const long n = (long)(zEnd - zStart) * ntr;
+        const int nar = c.na_ref;
+        sg->orientation = orientation;
+        sg->base = (long)zStart * ntr;
+        sg->n = n;
+        sg->Q = nullptr;
+        if (ppc < 1) {
+            c.err = "opx_cgc_mv_super: round(aL/dt) particles per cell must be >= 1";
+            rc = OPX_ERR_INVALID;
+        } else if (n > 0 && cudaMalloc(&sg->Q, sizeof(double) * (size_t)ppc * nar * n) != cudaSuccess) {
+            cudaGetLastError();
+            sg->Q = nullptr;
+            c.err = "opx_cgc_mv_super: out of device memory";
+            rc = OPX_ERR_NOMEM;
+        } else if (n > 0) {
+            if (nc == 2) k_super_init<2><<<grid_for(n, 128), 128, 0, c.stream>>>(Gv, V, ntr, sg->base, n, ppc, sg->Q);
+            else k_super_init<3><<<grid_for(n, 128), 128, 0, c.stream>>>(Gv, V, ntr, sg->base, n, ppc, sg->Q);
+            k_super_refine<<<grid_for(ntr, 64), 64, 0, c.stream>>>(sg->Q, nar, n, ntr, ppc, (long)(zEnd - zStart) * ppc);
+            c.launches += 2;
+            cudaError_t e = cudaStreamSynchronize(c.stream);
+            if (e != cudaSuccess) { c.err = std::string("opx_cgc_mv_super: ") + cudaGetErrorString(e); rc = OPX_ERR_CUDA; }
+        }
+    }
     // 4. particles (LightConeNGPParticleCreator.initializeParticles, :110-235)
-    if (!rc) {
+    if (!rc && !sg) {
         const int ppc = (int)std::lround(aL / c.L.dt);
         double gmax = 0.0;
         for (int z = 0; z < n0; z++) gmax = std::max(gmax, mx[z]);
@@ -550,6 +659,7 @@ extern "C" int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
         if (!(nuclei[q].width > 0) || !(nuclei[q].uvt >= 0)) { c.err = "opx_cgc_mv: width must be > 0 and the UV cutoff >= 0"; return OPX_ERR_INVALID; }
     }
     if (!g_fft.load(c.err)) return OPX_ERR_UNSUPPORTED;
+    if (!c.sg.empty()) { c.err = "opx_cgc_mv: the handle holds super particles (optimized CGC type)"; return OPX_ERR_INVALID; }
     // particles already on the handle stay first in the list (s.particles.add appends)
     const long n0 = c.P.n;
     const int nar = c.na_ref;
@@ -564,11 +674,42 @@ extern "C" int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
         opx_mv_nucleus nu = nuclei[k];
         // MVModel without randomSeed draws from an unseeded java.util.Random
         if (!nu.use_seed) nu.seed = (int)std::random_device{}();
-        int rc = cgc_nucleus(c, nu, p0, p1, v, q0, d);
+        int rc = cgc_nucleus(c, nu, p0, p1, v, q0, d, nullptr);
         if (rc) return rc;
     }
     // Q1 = Q0 for the new particles (LightConeNGPParticleCreator.java:229-234)
     q1.insert(q1.end(), q0.begin() + (size_t)nar * n0, q0.end());
     opx_particles P{(long)d.size(), p0.data(), p1.data(), v.data(), q0.data(), q1.data(), d.data(), nullptr};
     return opx_particles_upload(ctx, &P);
+}
+
+extern "C" int opx_cgc_mv_super(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
+    if (!ctx || !nuclei || n < 1) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    if (c.prec != OPX_F64) { c.err = "opx_cgc_mv_super: CGC initial conditions need an OPX_F64 handle"; return OPX_ERR_UNSUPPORTED; }
+    if (c.P.n > 0) { c.err = "opx_cgc_mv_super: the handle holds NGP particles (cgc ngp type)"; return OPX_ERR_INVALID; }
+    for (int q = 0; q < n; q++) {
+        if (nuclei[q].direction != 0) { c.err = "opx_cgc_mv_super: the beam must run along direction 0"; return OPX_ERR_UNSUPPORTED; }
+        if (nuclei[q].orientation != 1 && nuclei[q].orientation != -1) { c.err = "opx_cgc_mv_super: orientation must be +1 or -1"; return OPX_ERR_INVALID; }
+        if (!(nuclei[q].width > 0) || !(nuclei[q].uvt >= 0)) { c.err = "opx_cgc_mv_super: width must be > 0 and the UV cutoff >= 0"; return OPX_ERR_INVALID; }
+    }
+    if ((int)c.sg.size() + n > 32) { c.err = "opx_cgc_mv_super: at most 32 nuclei"; return OPX_ERR_INVALID; }
+    if (!g_fft.load(c.err)) return OPX_ERR_UNSUPPORTED;
+    const int ppc = (int)std::lround(c.L.a[0] / c.L.dt);
+    if (ppc < 1 || (int)(c.sg.size() + n) * ppc > 64) {
+        c.err = "opx_cgc_mv_super: round(aL/dt) must be >= 1 and nuclei x round(aL/dt) <= 64";
+        return OPX_ERR_INVALID;
+    }
+    std::vector<double> p0, p1, v, q0;
+    std::vector<int32_t> d;
+    for (int k = 0; k < n; k++) {
+        opx_mv_nucleus nu = nuclei[k];
+        if (!nu.use_seed) nu.seed = (int)std::random_device{}();
+        SuperGroup G;
+        int rc = cgc_nucleus(c, nu, p0, p1, v, q0, d, &G);
+        if (rc) { if (G.Q) cudaFree(G.Q); return rc; }
+        c.sg.push_back(G);
+    }
+    c.sg_ppc = ppc;
+    return OPX_OK;
 }

@@ -18,6 +18,8 @@
 // scatter), each bucket is put back into ascending particle order, and one
 // thread per key sums its bucket sequentially starting from 0.0 (resetCharge /
 // resetCurrent).  No floating-point atomics are used.
+#include <cmath>
+
 #include "internal.h"
 
 namespace opx {
@@ -344,6 +346,187 @@ void launch_cpic_phases(Ctx &c, int reassign) {
     else k_cpic_segsum<2><<<grid_for(n4, B), B, 0, c.stream>>>(P, V, (double *)c.rho, (double *)c.J);
     c.launches += 7;
     c.j_nonzero = true;
+}
+
+// ---------------------------------------------------------------- super particles
+// CGCSuperParticleInterpolationNGP (physics/grid/CGCSuperParticleInterpolationNGP.java):
+// the particles move along direction 0 with fixed relative positions; super
+// particle k of a group is a block of charges whose global cell index is
+// offset_k(t) + j.  The reference adds the super particles into rho and J in
+// list order (group by group, and within a group subdivision by subdivision,
+// k = 0 .. ppc-1); every cell then receives its terms in (group, k) order, the
+// order of the loops below, whatever the subdivision.  One thread per cell sums
+// them from 0.0, so the deposits are bit-exact.
+constexpr int SUPER_MAX = 64;
+struct SuperStep {
+    int m;                       // entries = groups x ppc, list order
+    long off[SUPER_MAX];         // offset_k(t) (current, or NGP for the charge density)
+    long n[SUPER_MAX];
+    const double *Q[SUPER_MAX];  // [na_ref][n] of this (group, k)
+    int orient[SUPER_MAX];
+    int upd[SUPER_MAX];          // needsUpdate(t)
+};
+
+template <int NC>
+__device__ __forceinline__ void ref_to_gen(const double *acc, double *g) {
+    if (NC == 3) {
+        // SU3AlgebraElement.get(a) (math/SU3AlgebraElement.java:117-129)
+        const double s3 = 1.7320508075688772;
+        g[0] = 2 * acc[1]; g[1] = 2 * acc[3]; g[2] = acc[0] - acc[4]; g[3] = 2 * acc[2];
+        g[4] = 2 * acc[6]; g[5] = 2 * acc[5]; g[6] = 2 * acc[7];
+        g[7] = (acc[0] + acc[4] - 2 * acc[8]) / s3;
+    } else {
+        g[0] = acc[0]; g[1] = acc[1]; g[2] = acc[2];
+    }
+}
+
+template <int NC>
+__device__ __forceinline__ void ref_act(const double *v, const double *u, double *out) {
+    if (NC == 3) ref_su3_act(v, u, out); else ref_su2_act(v, u, out);
+}
+template <int NC>
+__device__ __forceinline__ void ref_adj(const double *u, double *out) {
+    if (NC == 3) ref_su3_adj(u, out);
+    else { out[0] = u[0]; out[1] = -u[1]; out[2] = -u[2]; out[3] = -u[3]; }
+}
+
+// interpolateChargedensity (:75-93)
+template <int NC>
+__global__ void k_super_cin(SuperStep S, long V, double *__restrict__ rho) {
+    constexpr int NAR = NC == 3 ? 9 : 3, NA = NC == 3 ? 8 : 3;
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= V) return;
+    double acc[NAR];
+    for (int a = 0; a < NAR; a++) acc[a] = 0.0;
+    for (int e = 0; e < S.m; e++) {
+        const long j = c - S.off[e];
+        if (j < 0 || j >= S.n[e]) continue;
+        for (int a = 0; a < NAR; a++) acc[a] = acc[a] + S.Q[e][(long)a * S.n[e] + j];
+    }
+    double g[NA];
+    ref_to_gen<NC>(acc, g);
+    for (int a = 0; a < NA; a++) rho[(long)a * V + c] = g[a];
+}
+
+// interpolateToGrid (:19-73), the current along direction 0.  Orientation +1:
+// J(index + quickfix) += Q (as/at) with Q before its transport; orientation -1:
+// J(index) += (U Q U^dagger) (-as/at), U = Unext_0(index).  quickfix = one
+// plane when one particle sits in a cell (ppc = 1), and the last quickfix
+// cells are excluded for both orientations, as in the reference.
+template <int NC>
+__global__ void k_super_jin(SuperStep S, long V, long qf, double f, const double *__restrict__ Unext,
+                            double *__restrict__ J) {
+    constexpr int NAR = NC == 3 ? 9 : 3, NA = NC == 3 ? 8 : 3, NG = NC == 3 ? 18 : 4;
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= V) return;
+    double acc[NAR];
+    for (int a = 0; a < NAR; a++) acc[a] = 0.0;
+    for (int e = 0; e < S.m; e++) {
+        if (!S.upd[e]) continue;
+        if (S.orient[e] > 0) {
+            const long index = c - qf, j = index - S.off[e];
+            if (j < 0 || j >= S.n[e] || index < 0 || index >= V - qf) continue;
+            for (int a = 0; a < NAR; a++) acc[a] = acc[a] + S.Q[e][(long)a * S.n[e] + j] * f;
+        } else {
+            const long index = c, j = index - S.off[e];
+            if (j < 0 || j >= S.n[e] || index >= V - qf) continue;
+            double q[NAR], u[NG], t[NAR];
+            for (int a = 0; a < NAR; a++) q[a] = S.Q[e][(long)a * S.n[e] + j];
+            for (int k = 0; k < NG; k++) u[k] = Unext[link_offset(V, NG, 0, k, index)];
+            ref_act<NC>(q, u, t);
+            for (int a = 0; a < NAR; a++) acc[a] = acc[a] + t[a] * -f;
+        }
+    }
+    double g[NA];
+    ref_to_gen<NC>(acc, g);
+    for (int a = 0; a < NA; a++) J[(long)a * V + c] = g[a];
+}
+
+// the parallel transport of the charges that crossed (:59-60, :66-67)
+template <int NC>
+__global__ void k_super_transport(double *__restrict__ Q, long n, long off, int orientation, long V, long qf,
+                                  const double *__restrict__ Unext) {
+    constexpr int NAR = NC == 3 ? 9 : 3, NG = NC == 3 ? 18 : 4;
+    const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const long index = off + j;
+    if (index < 0 || index >= V - qf) return;
+    double q[NAR], u[NG], ua[NG], t[NAR];
+    for (int a = 0; a < NAR; a++) q[a] = Q[(long)a * n + j];
+    for (int k = 0; k < NG; k++) u[k] = Unext[link_offset(V, NG, 0, k, index)];
+    if (orientation > 0) {
+        ref_adj<NC>(u, ua);
+        ref_act<NC>(q, ua, t);
+    } else {
+        ref_act<NC>(q, u, t);
+    }
+    for (int a = 0; a < NAR; a++) Q[(long)a * n + j] = t[a];
+}
+
+// CGCSuperParticle.getCurrentOffset / getCurrentNGPOffset / needsUpdate (:71-105)
+static long super_offset(int orientation, long base, int shift, int ppc, long ppp, long t) {
+    if (orientation > 0) return base + ((t + shift) / ppc) * ppp;
+    return base + (long)std::floor((-t + shift) / (1.0 * ppc)) * ppp;
+}
+static long super_ngp_offset(int orientation, long base, int shift, int ppc, long ppp, long t) {
+    const long cur = super_offset(orientation, base, shift, ppc, ppp, t);
+    if (orientation > 0) return cur + ((((t + shift) % ppc) < ppc / 2) ? 0 : ppp);
+    return cur + ((((t - shift + ppc + ppc / 2 - 1) % ppc) < ppc / 2) ? 0 : ppp);
+}
+static bool super_needs_update(int orientation, int shift, int ppc, long t) {
+    if (orientation > 0) return 0 == (t + shift + ppc / 2 + 1) % ppc;
+    return 0 == (t - shift + ppc / 2) % ppc;
+}
+
+void launch_super_phases(Ctx &c, long t) {
+    const long V = c.L.V, ntr = V / c.L.n[0];
+    const int ppc = c.sg_ppc, nar = c.na_ref;
+    SuperStep cin{}, jin{};
+    int m = 0;
+    for (const SuperGroup &G : c.sg)
+        for (int k = 0; k < ppc && m < SUPER_MAX; k++, m++) {
+            const double *Qk = G.Q + (size_t)k * nar * G.n;
+            cin.off[m] = super_ngp_offset(G.orientation, G.base, k, ppc, ntr, t);
+            jin.off[m] = super_offset(G.orientation, G.base, k, ppc, ntr, t);
+            cin.n[m] = jin.n[m] = G.n;
+            cin.Q[m] = jin.Q[m] = Qk;
+            cin.orient[m] = jin.orient[m] = G.orientation;
+            cin.upd[m] = 1;
+            jin.upd[m] = super_needs_update(G.orientation, k, ppc, t) ? 1 : 0;
+        }
+    cin.m = jin.m = m;
+    const int B = 256;
+    const long qf = ppc == 1 ? ntr : 0;
+    const double f = c.L.a[0] / c.L.dt;
+    double *rho = (double *)c.rho, *J = (double *)c.J;
+    const double *Un = (const double *)c.Unext;
+    // resetCharge + interpolateChargedensity
+    if (c.nc == 3) k_super_cin<3><<<grid_for(V, B), B, 0, c.stream>>>(cin, V, rho);
+    else k_super_cin<2><<<grid_for(V, B), B, 0, c.stream>>>(cin, V, rho);
+    // resetCurrent + interpolateToGrid: J_0 from the crossing charges, then their transport
+    cudaMemsetAsync(J + (size_t)c.na * V, 0, sizeof(double) * 2 * c.na * V, c.stream);
+    if (c.nc == 3) k_super_jin<3><<<grid_for(V, B), B, 0, c.stream>>>(jin, V, qf, f, Un, J);
+    else k_super_jin<2><<<grid_for(V, B), B, 0, c.stream>>>(jin, V, qf, f, Un, J);
+    c.launches += 2;
+    int e = 0;
+    for (SuperGroup &G : c.sg)
+        for (int k = 0; k < ppc && e < SUPER_MAX; k++, e++) {
+            if (!jin.upd[e]) continue;
+            double *Qk = G.Q + (size_t)k * nar * G.n;
+            if (c.nc == 3)
+                k_super_transport<3><<<grid_for(G.n, B), B, 0, c.stream>>>(Qk, G.n, jin.off[e], G.orientation, V, qf, Un);
+            else
+                k_super_transport<2><<<grid_for(G.n, B), B, 0, c.stream>>>(Qk, G.n, jin.off[e], G.orientation, V, qf, Un);
+            c.launches++;
+        }
+    c.j_nonzero = true;
+}
+
+void super_free(Ctx &c) {
+    for (SuperGroup &G : c.sg)
+        if (G.Q) cudaFree(G.Q);
+    c.sg.clear();
+    c.sg_ppc = 0;
 }
 
 }  // namespace opx

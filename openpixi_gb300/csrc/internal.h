@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/opixi.h"
 #include "lattice.cuh"
@@ -32,6 +33,15 @@ struct Particles {
     long scan_tmp_len = 0;
 };
 
+// Super particles (CGCSuperParticle, temporal optimized cgc ngp): one group per
+// nucleus, ppc layers k of charges over the particle block [base, base + n)
+// of global cell indices; Q is [ppc][na_ref][n] on the device.
+struct SuperGroup {
+    int orientation = 1;
+    long n = 0, base = 0;
+    double *Q = nullptr;
+};
+
 struct Ctx {
     opx_config cfg;
     Lat L;
@@ -56,6 +66,8 @@ struct Ctx {
     long steps = 0;
     long launches = 0;
     Particles P;
+    std::vector<SuperGroup> sg;  // super-particle groups in list order
+    int sg_ppc = 0;
     bool profiling = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double phase_ms[OPX_NUM_PHASES] = {0, 0, 0, 0};
@@ -86,6 +98,8 @@ int ic_gauss_project(Ctx &c, double tol, int maxit, int *iters, double *final_g2
 int cpic_alloc(Ctx &c, long n);
 void cpic_free(Ctx &c);
 void launch_cpic_phases(Ctx &c, int reassign);
+void launch_super_phases(Ctx &c, long t);  // CGCSuperParticleInterpolationNGP CIN + JIN at step t
+void super_free(Ctx &c);
 
 int grid_for(long n, int block);
 

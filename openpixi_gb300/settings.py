@@ -20,7 +20,7 @@ SIMULATION_TYPES = {
 }
 # simulation types whose solver/interpolator combination this library provides
 # (Settings.applySimulationTypeSetting, physics/Settings.java:540-581)
-SUPPORTED = {"TemporalYangMills", "TemporalCGCNGP"}
+SUPPORTED = {"TemporalYangMills", "TemporalCGCNGP", "TemporalOptimizedCGCNGP"}
 
 
 class Settings:

@@ -251,7 +251,13 @@ class Simulation:
         self.particles = len(direction)
 
     def get_particles(self):
-        return self.grid.handle.particles_download() if self.particles else None
+        """NGP particles as arrays, or the super-particle groups (optimized CGC type)."""
+        if not self.particles:
+            return None
+        h = self.grid.handle
+        if self.simulationType == "TemporalOptimizedCGCNGP":
+            return [h.super_download(k) for k in range(h.super_groups)]
+        return h.particles_download()
 
     def initialize(self):
         """Simulation.initialize: Unext from E, then the particle phases without reassign."""

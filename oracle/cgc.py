@@ -93,9 +93,10 @@ def poisson2d(rho, dims, aT):
     return np.fft.ifft2(f, axes=(1, 2)).real.reshape(-1)
 
 
-def mv_nucleus(grid: OracleGrid, nu: MVNucleus):
+def mv_nucleus(grid: OracleGrid, nu: MVNucleus, super_particles=False):
     """CGCInitialCondition.applyInitialCondition for one MVModel: updates the
-    grid's U, Unext, E and returns the new particles (OracleParticles)."""
+    grid's U, Unext, E and returns the new particles (OracleParticles), or the
+    nucleus's super-particle group (SuperGroup) for the optimized simulation type."""
     if nu.direction != 0:
         raise ValueError("the particle creator assumes the beam along dimension 0")
     L = lib()
@@ -121,6 +122,8 @@ def mv_nucleus(grid: OracleGrid, nu: MVNucleus):
     L.orc_cgc_solve.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 6
     L.orc_cgc_solve(grid.pp, 0, int(nu.orientation), _p(phi), _p(grid.U), _p(grid.Unext), _p(grid.E),
                     _p(grid.active), _p(gauss))
+    if super_particles:
+        return super_group(grid, gauss, int(nu.orientation)), {"rho": rho, "phi": phi, "gauss": gauss}
     L.orc_cgc_particles.restype = C.c_long
     L.orc_cgc_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_long] + [C.c_void_p] * 4
     n = L.orc_cgc_particles(grid.pp, _p(gauss), int(nu.orientation), 0, None, None, None, None)
@@ -131,6 +134,84 @@ def mv_nucleus(grid: OracleGrid, nu: MVNucleus):
     P.Q1[...] = P.Q0
     P.dir[...] = 0
     return P, {"rho": rho, "phi": phi, "gauss": gauss}
+
+
+class SuperGroup:
+    """The super particles of one nucleus (LightConeNGPSuperParticleCreator):
+    Q[k][i] is charge i of super particle k, i over the particle block
+    [base, base + n) of global cell indices."""
+
+    def __init__(self, orientation, n, base, Q):
+        self.orientation = orientation
+        self.n = n
+        self.base = base
+        self.Q = Q
+
+
+def super_group(grid, gauss, orientation):
+    L = lib()
+    L.orc_super_create.restype = C.c_long
+    L.orc_super_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    base = C.c_long()
+    n = L.orc_super_create(grid.pp, _p(gauss), C.byref(base), None)
+    if n < 0:
+        raise ValueError("round(aL/dt) particles per cell must be >= 1")
+    ppc = int(round(grid.a[0] / grid.dt))
+    Q = np.zeros((ppc, max(n, 1), na(grid.nc)))
+    L.orc_super_create(grid.pp, _p(gauss), C.byref(base), _p(Q))
+    return SuperGroup(orientation, n, base.value, Q)
+
+
+class OracleSuperSimulation:
+    """Simulation.initialize/step (physics/Simulation.java:318-435) for the
+    optimized CGC type: field update, then CGCSuperParticleInterpolationNGP's
+    charge density and current (the particle solver does nothing)."""
+
+    def __init__(self, grid, groups, nthreads=1):
+        self.grid = grid
+        self.groups = groups
+        self.nthreads = nthreads
+        self.steps = 0
+
+    def _args(self):
+        k = len(self.groups)
+        orient = (C.c_int * k)(*[g.orientation for g in self.groups])
+        n = (C.c_long * k)(*[g.n for g in self.groups])
+        base = (C.c_long * k)(*[g.base for g in self.groups])
+        Q = (C.c_void_p * k)(*[g.Q.ctypes.data for g in self.groups])
+        return k, orient, n, base, Q
+
+    def _phases(self, t):
+        g, L = self.grid, lib()
+        k, orient, n, base, Q = self._args()
+        L.orc_super_cin.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int, C.c_long, C.c_void_p]
+        L.orc_super_jin.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int, C.c_long, C.c_void_p, C.c_void_p]
+        g.rho[...] = 0.0
+        L.orc_super_cin(g.pp, k, orient, n, base, Q, self.nthreads, t, _p(g.rho))
+        g.J[...] = 0.0
+        L.orc_super_jin(g.pp, k, orient, n, base, Q, self.nthreads, t, _p(g.Unext), _p(g.J))
+
+    def initialize(self):
+        self.grid.update_links()
+        self._phases(0)
+
+    def step(self):
+        self.steps += 1
+        self.grid.store_fields()
+        self.grid.update_grid()
+        self._phases(self.steps)
+
+
+def cgc_mv_super(grid: OracleGrid, nuclei):
+    """All nuclei in order, with super particles (simulationType temporal optimized cgc ngp)."""
+    groups, info = [], []
+    for nu in nuclei:
+        G, d = mv_nucleus(grid, nu, super_particles=True)
+        groups.append(G)
+        info.append(d)
+    return groups, info
 
 
 def concat(parts, nc):

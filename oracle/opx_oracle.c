@@ -1479,3 +1479,227 @@ long orc_cgc_particles(const orc_params *p, const double *gauss, int orientation
     }
     return np;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Super particles (physics/particles/CGCSuperParticle.java,                  */
+/* physics/grid/CGCSuperParticleInterpolationNGP.java,                        */
+/* physics/initial/CGC/LightConeNGPSuperParticleCreator.java)                 */
+/* ------------------------------------------------------------------------- */
+
+/* LightConeNGPSuperParticleCreator.initializeParticles (:102-241) for the
+ * beam along direction 0.  The charges of super particle k (k < ppc) over the
+ * whole particle block, index i = global cell index - base, are written to
+ * Q[k][i][na]; the block is [base, base + n) with base = zStart * ntr and
+ * n = (zEnd - zStart) * ntr.  The subdivision of the block into
+ * numberOfThreads pieces only splits these arrays (orc_super_cin/jin take it
+ * as a parameter).  Returns n (Q filled when Q != NULL); *base_out = base. */
+long orc_super_create(const orc_params *p, const double *gauss, long *base_out, double *Q)
+{
+    int nc = p->nc, na = orc_na(nc);
+    long V = vol(p);
+    int lnum = p->n[0];
+    long ntr = V / lnum;
+    int ppc = (int)lround(p->a[0] / p->dt);
+    if (ppc < 1) return -1;
+    double *maxCharges = malloc(sizeof(double) * lnum), globalMax = 0.0;
+    for (int z = 0; z < lnum; z++) {
+        double mx = 0.0;
+        for (long j = 0; j < ntr; j++) {
+            double charge = sqrt(orc_alg_square(nc, gauss + (size_t)(z * ntr + j) * na));
+            if (mx < charge) mx = charge;
+        }
+        maxCharges[z] = mx;
+        if (globalMax < mx) globalMax = mx;
+    }
+    double cutoff = globalMax * 10E-10;
+    int zStart = 0, zEnd = lnum - 1;
+    for (int z = 0; z < lnum; z++) if (maxCharges[z] > cutoff) { zStart = z; break; }
+    for (int z = zEnd - 1; z >= 0; z--) if (maxCharges[z] > cutoff) { zEnd = z; break; }
+    free(maxCharges);
+    long blockWidth = zEnd - zStart, n = blockWidth * ntr;
+    long base = (long)zStart * ntr;
+    if (base_out) *base_out = base;
+    if (!Q) return n;
+    for (long i = 0; i < n; i++) {
+        long index = base + i;
+        for (int k = 0; k < ppc; k++) {
+            long ngp = (k < ppc / 2) ? index : orc_shift(p, index, 0, 1);
+            for (int a = 0; a < na; a++)
+                Q[((size_t)k * n + i) * na + a] = gauss[(size_t)ngp * na + a] * (1.0 / ppc);
+        }
+    }
+    /* refinement over each transverse column's longitudinal list
+     * (:200-240): entry (zrel * ppc + k) is charge i = zrel * ntr + t of super particle k */
+    long len = blockWidth * ppc;
+    for (long t = 0; t < ntr && len > 0; t++) {
+#define SQ(ii) (Q + ((size_t)(ring((ii), len) % ppc) * n + (ring((ii), len) / ppc) * ntr + t) * na)
+        for (int it = 0; it < 100; it++)
+            for (long i = 0; i < len; i++) {
+                long jm = (i + ppc / 2) % ppc;
+                if (!(jm >= 0 && jm < ppc - 1)) continue;
+                double *Q0 = SQ(i - 1), *Q1 = SQ(i), *Q2 = SQ(i + 1), *Q3 = SQ(i + 2);
+                for (int a = 0; a < na; a++) {
+                    double DQ = Q0[a] * -1;
+                    DQ = DQ + Q1[a] * 3;
+                    DQ = DQ + Q2[a] * -3;
+                    DQ = DQ + Q3[a] * 1;
+                    DQ = DQ * (1.0 / 4.0);
+                    Q1[a] = Q1[a] + DQ * -1.0;
+                    Q2[a] = Q2[a] + DQ * 1.0;
+                }
+            }
+        for (int it = 0; it < 100; it++)
+            for (long i = 0; i < len; i++) {
+                long jm = (i + ppc / 2) % ppc;
+                if (!(jm >= 0 && jm < ppc - 1)) continue;
+                double *Q0 = SQ(i - 2), *Q1 = SQ(i - 1), *Q2 = SQ(i), *Q3 = SQ(i + 1), *Q4 = SQ(i + 2),
+                       *Q5 = SQ(i + 3);
+                for (int a = 0; a < na; a++) {
+                    double DQ = Q0[a] * 1;
+                    DQ = DQ + Q1[a] * -5;
+                    DQ = DQ + Q2[a] * 10;
+                    DQ = DQ + Q3[a] * -10;
+                    DQ = DQ + Q4[a] * 5;
+                    DQ = DQ + Q5[a] * -1;
+                    DQ = DQ * (1.0 / 12.0);
+                    Q2[a] = Q2[a] + DQ * -1.0;
+                    Q3[a] = Q3[a] + DQ * 1.0;
+                }
+            }
+#undef SQ
+    }
+    return n;
+}
+
+/* One super particle as the reference holds it. */
+typedef struct {
+    int orientation, numberOfParticles, particlesPerPlane, subLatticeShift, particlePerCell;
+    long indexOffset;
+    double *Q; /* [numberOfParticles][na] */
+} super_particle;
+
+/* CGCSuperParticle.getCurrentOffset / getCurrentNGPOffset / needsUpdate (:71-105) */
+static long sp_offset(const super_particle *P, long t)
+{
+    if (P->orientation > 0)
+        return P->indexOffset + ((t + P->subLatticeShift) / P->particlePerCell) * P->particlesPerPlane;
+    long shift = (long)floor((-t + P->subLatticeShift) / (1.0 * P->particlePerCell)) * P->particlesPerPlane;
+    return P->indexOffset + shift;
+}
+static long sp_ngp_offset(const super_particle *P, long t)
+{
+    long cur = sp_offset(P, t);
+    int ppc = P->particlePerCell;
+    if (P->orientation > 0)
+        return cur + ((((t + P->subLatticeShift) % ppc) < ppc / 2) ? 0 : P->particlesPerPlane);
+    return cur + ((((t - P->subLatticeShift + ppc + ppc / 2 - 1) % ppc) < ppc / 2) ? 0 : P->particlesPerPlane);
+}
+static int sp_needs_update(const super_particle *P, long t)
+{
+    int ppc = P->particlePerCell;
+    if (P->orientation > 0) return 0 == (t + P->subLatticeShift + ppc / 2 + 1) % ppc;
+    return 0 == (t - P->subLatticeShift + ppc / 2) % ppc;
+}
+
+/* The super particles of one group (one nucleus) in the reference's list
+ * order for numberOfThreads = nthreads (:153-195): subdivision j of the block,
+ * then k = 0 .. ppc-1.  Returns the count written to out (<= cap). */
+static int sp_list(const orc_params *p, int orientation, long n, long base, double *Q, int nthreads,
+                   super_particle *out, int cap)
+{
+    int na = orc_na(p->nc);
+    long ntr = vol(p) / p->n[0];
+    int ppc = (int)lround(p->a[0] / p->dt);
+    long blockWidth = n / ntr;
+    if (blockWidth <= 0) return 0;
+    long nsub = nthreads < blockWidth ? nthreads : blockWidth;
+    long ws = blockWidth / nsub, wl = blockWidth / nsub + 1;
+    long ps = ws * ntr, pl = wl * ntr;
+    long nl = blockWidth - nsub * ws;
+    long off = 0;
+    int m = 0;
+    for (long j = 0; j < nsub; j++) {
+        long cnt = j < nl ? pl : ps;
+        for (int k = 0; k < ppc && m < cap; k++, m++) {
+            super_particle *P = out + m;
+            P->orientation = orientation;
+            P->numberOfParticles = (int)cnt;
+            P->indexOffset = base + off;
+            P->particlesPerPlane = (int)ntr;
+            P->subLatticeShift = k;
+            P->particlePerCell = ppc;
+            P->Q = Q + ((size_t)k * n + off) * na;
+        }
+        off += cnt;
+    }
+    return m;
+}
+
+/* CGCSuperParticleInterpolationNGP.interpolateChargedensity (:75-93) over all
+ * groups in list order.  Groups: orient[g], n[g], base[g], Q[g] ([ppc][n][na]). */
+void orc_super_cin(const orc_params *p, int ngroups, const int *orient, const long *n, const long *base,
+                   double *const *Q, int nthreads, long t, double *rho)
+{
+    int na = orc_na(p->nc);
+    long V = vol(p);
+    super_particle list[4096];
+    for (int g = 0; g < ngroups; g++) {
+        int m = sp_list(p, orient[g], n[g], base[g], Q[g], nthreads, list, 4096);
+        for (int q = 0; q < m; q++) {
+            const super_particle *P = list + q;
+            long indexOffset = sp_ngp_offset(P, t);
+            long imin = (indexOffset < 0) ? -indexOffset : 0;
+            long hi = indexOffset + P->numberOfParticles < V ? indexOffset + P->numberOfParticles : V;
+            long imax = hi - indexOffset > 0 ? hi - indexOffset : 0;
+            long ireg = imax - imin;
+            for (long i = 0; i < ireg; i++) {
+                long j = i + imin, index = indexOffset + j;
+                for (int a = 0; a < na; a++)
+                    rho[(size_t)index * na + a] = rho[(size_t)index * na + a] + P->Q[(size_t)j * na + a];
+            }
+        }
+    }
+}
+
+/* CGCSuperParticleInterpolationNGP.interpolateToGrid (:19-73): for the super
+ * particles that cross an NGP boundary in the next step, the current along
+ * direction 0 and the parallel transport of their charges by Unext. */
+void orc_super_jin(const orc_params *p, int ngroups, const int *orient, const long *n, const long *base,
+                   double *const *Q, int nthreads, long t, const double *Unext, double *J)
+{
+    int nc = p->nc, na = orc_na(nc), ng = orc_ng(nc);
+    long V = vol(p);
+    double at = p->dt, as = p->a[0];
+    super_particle list[4096];
+    for (int g = 0; g < ngroups; g++) {
+        int m = sp_list(p, orient[g], n[g], base[g], Q[g], nthreads, list, 4096);
+        for (int q = 0; q < m; q++) {
+            const super_particle *P = list + q;
+            if (!sp_needs_update(P, t)) continue;
+            long indexOffset = sp_offset(P, t);
+            long quickfix = P->particlePerCell == 1 ? P->particlesPerPlane : 0;
+            long imin = (indexOffset < 0) ? -indexOffset : 0;
+            long hi = indexOffset + P->numberOfParticles < V - quickfix ? indexOffset + P->numberOfParticles
+                                                                        : V - quickfix;
+            long imax = hi - indexOffset > 0 ? hi - indexOffset : 0;
+            long ireg = imax - imin;
+            for (long i = 0; i < ireg; i++) {
+                long j = i + imin, index = indexOffset + j;
+                double *Qj = P->Q + (size_t)j * na, tmp[NA_MAX], g2[NG_MAX];
+                const double *Ul = Unext + ((size_t)index * 3 + 0) * ng;
+                if (P->orientation > 0) {
+                    double *Jc = J + ((size_t)(index + quickfix) * 3 + 0) * na;
+                    for (int a = 0; a < na; a++) Jc[a] = Jc[a] + Qj[a] * (as / at);
+                    orc_group_adj(nc, Ul, g2);
+                    orc_alg_act(nc, Qj, g2, tmp);
+                    memcpy(Qj, tmp, sizeof(double) * na);
+                } else {
+                    orc_alg_act(nc, Qj, Ul, tmp);
+                    memcpy(Qj, tmp, sizeof(double) * na);
+                    double *Jc = J + ((size_t)index * 3 + 0) * na;
+                    for (int a = 0; a < na; a++) Jc[a] = Jc[a] + Qj[a] * (-as / at);
+                }
+            }
+        }
+    }
+}

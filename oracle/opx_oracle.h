@@ -154,6 +154,13 @@ void orc_cgc_solve(const orc_params *p, int direction, int orientation, const do
 long orc_cgc_particles(const orc_params *p, const double *gauss, int orientation, long cap,
                        double *pos0, double *pos1, double *vel, double *Q);
 
+/* ---- super particles (temporal optimized cgc ngp) ---- */
+long orc_super_create(const orc_params *p, const double *gauss, long *base_out, double *Q);
+void orc_super_cin(const orc_params *p, int ngroups, const int *orient, const long *n, const long *base,
+                   double *const *Q, int nthreads, long t, double *rho);
+void orc_super_jin(const orc_params *p, int ngroups, const int *orient, const long *n, const long *base,
+                   double *const *Q, int nthreads, long t, const double *Unext, double *J);
+
 #ifdef __cplusplus
 }
 #endif

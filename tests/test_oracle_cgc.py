@@ -90,3 +90,33 @@ def test_particle_layout(orc, cgc):
     assert np.array_equal(P.pos0[:, 1], np.floor(P.pos0[:, 1]) + 1e-11) or np.allclose(P.pos0[:, 1], t // 4 + 1e-11)
     assert np.allclose(P.pos1[:, 0] - P.pos0[:, 0], -0.25)
     assert np.all(P.vel[:, 0] == -1.0) and np.all(P.vel[:, 1:] == 0.0)
+
+
+def test_super_particles_subdivision_invariant_and_gauss(orc, cgc):
+    """LightConeNGPSuperParticleCreator + CGCSuperParticleInterpolationNGP: the
+    result does not depend on how the particle block is split among threads
+    (numberOfThreads), the Gauss law holds through the run, and the physics
+    agrees with the NGP particles of the same nuclei."""
+    nuclei = [cgc.MVNucleus(orientation=1, location=12.0, width=1.5, mu=0.5, seed=3),
+              cgc.MVNucleus(orientation=-1, location=28.0, width=1.5, mu=0.5, seed=4)]
+    runs = []
+    for nt in (1, 3, 7):
+        g = orc.OracleGrid(2, (40, 6, 6), dt=0.5)
+        groups, _ = cgc.cgc_mv_super(g, nuclei)
+        sim = cgc.OracleSuperSimulation(g, groups, nthreads=nt)
+        sim.initialize()
+        g0 = np.abs(g.gauss_field()).max()
+        for _ in range(12):
+            sim.step()
+        assert np.abs(g.gauss_field()).max() <= 1.01 * g0 + 1e-12
+        runs.append((g.U.copy(), g.E.copy(), g.J.copy()))
+    for r in runs[1:]:
+        for a, b in zip(r, runs[0]):
+            assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    g2 = orc.OracleGrid(2, (40, 6, 6), dt=0.5)
+    P, _ = cgc.cgc_mv(g2, nuclei)
+    s2 = orc.OracleSimulation(g2, P)
+    s2.initialize()
+    for _ in range(12):
+        s2.step()
+    assert np.abs(runs[0][0] - g2.U).max() < 1e-3
