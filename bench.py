@@ -379,6 +379,29 @@ def bench_cgc(device, nsteps=300, oracle_steps=2):
            "roofline_frac_eom": 136.0 * links / (ms[N.PHASE_EOM] / nsteps / 1000.0) / 1e9 / peak,
            "bytes_per_link": 136, "max_gauss_mean_sq": gmax, "energy_start": e0, "energy_end": e1,
            "projected_energy_rows": [4, CGC_DIMS[0]], "final_T_el_sum": float(proj[-1][0].sum())}
+    # the same collision with super particles (temporal optimized cgc ngp)
+    try:
+        hs = opx.Handle(2, CGC_DIMS, a=1.0, dt=0.5, g=1.0, precision=N.OPX_F64, device=device)
+        hs.synchronize()
+        t = time.perf_counter()
+        hs.cgc_mv_super(cgc_nuclei())
+        hs.synchronize()
+        sic = 1000.0 * (time.perf_counter() - t)
+        hs.initialize()
+        hs.set_profiling(True)
+        hs.step(nsteps)
+        sms, _ = hs.phase_times()
+        hs.set_profiling(False)
+        so = hs.reduce()
+        charges = sum(hs.super_download(k)["n"] for k in range(hs.super_groups)) * 2
+        out["super_particles"] = {
+            "groups": hs.super_groups, "charges": charges, "ic_ms": sic,
+            "eom_ms_per_step": sms[N.PHASE_EOM] / nsteps, "cpic_ms_per_step": sms[N.PHASE_CPIC] / nsteps,
+            "energy_end": so.e2_total + so.b2_total, "gauss_end": so.gauss,
+            "energy_end_rel_to_ngp": abs(so.e2_total + so.b2_total - e1) / e1}
+        hs.close()
+    except Exception as e:
+        out["super_particles"] = f"skipped: {e}"
     # oracle at full size: the initial condition and the first steps
     try:
         import oracle
