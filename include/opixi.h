@@ -192,6 +192,17 @@ typedef struct {
  * handles, beam along direction 0.  Call opx_initialize afterwards. */
 int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
 
+/* ---- occupation numbers (diagnostics/methods/OccupationNumbersInTime.java:172-297) ----
+ * On copies of the handle's fields: the Coulomb gauge iteration of
+ * CoulombGauge.applyGaugeTransformation (physics/gauge/CoulombGauge.java:56-194;
+ * at most max_iter iterations, until the summed squared divergence of
+ * A = log U falls below accuracy_goal; the reference uses 100 and 1e-18),
+ * then the occupation numbers n [V][3] (momentum index in cell order, colour
+ * inner) and the energy density from them.  n_out may be NULL.  SU(2), one
+ * lattice spacing; the optional mirrored grid and cone windows are not provided. */
+int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accuracy_goal, double *n_out, size_t count,
+                           double *energy_density, int *iterations, double *last_divergence);
+
 /* ---- super particles: simulationType "temporal optimized cgc ngp"
  *      (Settings.java:566-571: CGCSuperParticleSolver + CGCSuperParticleInterpolationNGP;
  *      physics/particles/CGCSuperParticle.java) ----

@@ -43,7 +43,7 @@ EXPORTED = [
     "opx_batch_kernel_launches",
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
     "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
-    "opx_super_download", "opx_super_upload",
+    "opx_super_download", "opx_super_upload", "opx_occupation_numbers",
 ]
 
 
@@ -148,6 +148,7 @@ def load(path=None):
         "opx_super_groups": (C.c_int, [vp]),
         "opx_super_download": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, C.c_size_t]),
         "opx_super_upload": (C.c_int, [vp, C.c_int, C.c_long, C.c_long, vp]),
+        "opx_occupation_numbers": (C.c_int, [vp, C.c_int, C.c_double, vp, C.c_size_t, vp, vp, vp]),
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
         "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
@@ -333,6 +334,14 @@ class Handle:
                 setattr(arr[k], f, nu[f])
         self.check(self.L.opx_cgc_mv(self.h, arr, len(nuclei)))
         self.np = self.L.opx_particles_count(self.h)
+
+    def occupation_numbers(self, max_iter=100, accuracy_goal=1e-18, with_n=True):
+        """OccupationNumbersInTime: (n [V][3] or None, energy density, iterations, last divergence)."""
+        n = np.empty((self.V, 3)) if with_n else None
+        e, it, dv = C.c_double(), C.c_int(), C.c_double()
+        self.check(self.L.opx_occupation_numbers(self.h, int(max_iter), float(accuracy_goal), ptr(n),
+                                                 0 if n is None else n.size, C.byref(e), C.byref(it), C.byref(dv)))
+        return n, e.value, it.value, dv.value
 
     # ---- super particles (temporal optimized cgc ngp) ----
     def cgc_mv_super(self, nuclei):

@@ -32,35 +32,13 @@
 
 #include <cufft.h>
 
+#include "fftlib.h"
 #include "internal.h"
 #include "java_random.h"
 
 namespace opx {
 
-// ---------------------------------------------------------------- cuFFT at run time
-struct FFTLib {
-    void *h = nullptr;
-    decltype(&cufftPlanMany) planMany = nullptr;
-    decltype(&cufftExecZ2Z) execZ2Z = nullptr;
-    decltype(&cufftSetStream) setStream = nullptr;
-    decltype(&cufftDestroy) destroy = nullptr;
-    bool load(std::string &err) {
-        if (h) return true;
-        const char *names[] = {"libcufft.so.12", "libcufft.so", "/usr/local/cuda/lib64/libcufft.so.12"};
-        for (const char *n : names) {
-            h = dlopen(n, RTLD_NOW | RTLD_LOCAL);
-            if (h) break;
-        }
-        if (!h) { err = "cuFFT library not found (libcufft.so.12)"; return false; }
-        planMany = (decltype(planMany))dlsym(h, "cufftPlanMany");
-        execZ2Z = (decltype(execZ2Z))dlsym(h, "cufftExecZ2Z");
-        setStream = (decltype(setStream))dlsym(h, "cufftSetStream");
-        destroy = (decltype(destroy))dlsym(h, "cufftDestroy");
-        if (!planMany || !execZ2Z || !setStream || !destroy) { err = "cuFFT symbols missing"; h = nullptr; return false; }
-        return true;
-    }
-};
-static FFTLib g_fft;
+
 
 // ---------------------------------------------------------------- kernels
 // V = identity in the direction-0 slot of a link-shaped buffer
@@ -442,15 +420,6 @@ __global__ void k_super_refine(double *__restrict__ Q, int nar, long n, long ntr
 
 using namespace opx;
 
-namespace {
-
-struct Plan {
-    cufftHandle h = 0;
-    bool ok = false;
-    ~Plan() { if (ok) g_fft.destroy(h); }
-};
-
-}  // namespace
 
 // Host driver; returns the particles created for this nucleus (reference layout, host).
 static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &ppos0, std::vector<double> &ppos1,
@@ -478,13 +447,11 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
     al((void **)&Gv, sizeof(double) * NA * V);
     al((void **)&smax, sizeof(double) * n0);
     int rc = OPX_OK;
-    Plan p3, p2;
+    FFTPlan p3, p2;
     if (ok) {
         int dims3[3] = {n0, n1, n2}, dims2[2] = {n1, n2};
-        p3.ok = g_fft.planMany(&p3.h, 3, dims3, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2Z, 1) == CUFFT_SUCCESS;
-        p2.ok = g_fft.planMany(&p2.h, 2, dims2, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2Z, n0) == CUFFT_SUCCESS;
-        if (p3.ok) g_fft.setStream(p3.h, c.stream);
-        if (p2.ok) g_fft.setStream(p2.h, c.stream);
+        p3.make(3, dims3, 1, c.stream);
+        p2.make(2, dims2, n0, c.stream);
     }
     if (!ok || !p3.ok || !p2.ok) {
         c.err = "opx_cgc_mv: out of device memory or cuFFT plan failure";
@@ -512,9 +479,9 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
             }
             cudaMemcpyAsync(phi, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice, c.stream);
             k_to_complex<<<grid_for(V, B), B, 0, c.stream>>>(phi, f, V);
-            if (g_fft.execZ2Z(p3.h, f, f, CUFFT_FORWARD) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
+            if (fft_lib().execZ2Z(p3.h, f, f, CUFFT_FORWARD) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
             k_regulate<<<grid_for(V, B), B, 0, c.stream>>>(f, n0, n1, n2, nu.uvt, nu.coherence, nu.ir, aT, aL);
-            if (g_fft.execZ2Z(p3.h, f, f, CUFFT_INVERSE) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
+            if (fft_lib().execZ2Z(p3.h, f, f, CUFFT_INVERSE) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
             k_from_complex<<<grid_for(V, B), B, 0, c.stream>>>(f, 1.0 / V, rho, comp, NA, V, n0, lmin, lmax, c.active);
             cudaStreamSynchronize(c.stream);
             c.launches += 4;
@@ -522,9 +489,9 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
         // 2. Poisson 2D per sheet (LightConePoissonSolverImproved.java:69-95)
         for (int comp = 0; comp < NA && !rc; comp++) {
             k_to_complex<<<grid_for(V, B), B, 0, c.stream>>>(rho + (long)comp * V, f, V);
-            if (g_fft.execZ2Z(p2.h, f, f, CUFFT_FORWARD) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
+            if (fft_lib().execZ2Z(p2.h, f, f, CUFFT_FORWARD) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
             k_poisson2d<<<grid_for(V, B), B, 0, c.stream>>>(f, n0, n1, n2, aT);
-            if (g_fft.execZ2Z(p2.h, f, f, CUFFT_INVERSE) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
+            if (fft_lib().execZ2Z(p2.h, f, f, CUFFT_INVERSE) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
             k_from_complex<<<grid_for(V, B), B, 0, c.stream>>>(f, 1.0 / ntr, phi, comp, NA, V, n0, -1, -1, nullptr);
             c.launches += 4;
         }
@@ -658,7 +625,7 @@ extern "C" int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
         if (nuclei[q].orientation != 1 && nuclei[q].orientation != -1) { c.err = "opx_cgc_mv: orientation must be +1 or -1"; return OPX_ERR_INVALID; }
         if (!(nuclei[q].width > 0) || !(nuclei[q].uvt >= 0)) { c.err = "opx_cgc_mv: width must be > 0 and the UV cutoff >= 0"; return OPX_ERR_INVALID; }
     }
-    if (!g_fft.load(c.err)) return OPX_ERR_UNSUPPORTED;
+    if (!fft_lib().load(c.err)) return OPX_ERR_UNSUPPORTED;
     if (!c.sg.empty()) { c.err = "opx_cgc_mv: the handle holds super particles (optimized CGC type)"; return OPX_ERR_INVALID; }
     // particles already on the handle stay first in the list (s.particles.add appends)
     const long n0 = c.P.n;
@@ -694,7 +661,7 @@ extern "C" int opx_cgc_mv_super(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int 
         if (!(nuclei[q].width > 0) || !(nuclei[q].uvt >= 0)) { c.err = "opx_cgc_mv_super: width must be > 0 and the UV cutoff >= 0"; return OPX_ERR_INVALID; }
     }
     if ((int)c.sg.size() + n > 32) { c.err = "opx_cgc_mv_super: at most 32 nuclei"; return OPX_ERR_INVALID; }
-    if (!g_fft.load(c.err)) return OPX_ERR_UNSUPPORTED;
+    if (!fft_lib().load(c.err)) return OPX_ERR_UNSUPPORTED;
     const int ppc = (int)std::lround(c.L.a[0] / c.L.dt);
     if (ppc < 1 || (int)(c.sg.size() + n) * ppc > 64) {
         c.err = "opx_cgc_mv_super: round(aL/dt) must be >= 1 and nuclei x round(aL/dt) <= 64";

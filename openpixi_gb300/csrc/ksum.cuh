@@ -8,13 +8,13 @@ namespace opx {
 struct KSum {
     double s, c;
 };
-__device__ __forceinline__ void two_sum_add(KSum &a, double x) {
+__host__ __device__ __forceinline__ void two_sum_add(KSum &a, double x) {
     double t = a.s + x;
     double z = t - a.s;
     a.c += (a.s - (t - z)) + (x - z);
     a.s = t;
 }
-__device__ __forceinline__ void ksum_merge(KSum &a, const KSum &b) {
+__host__ __device__ __forceinline__ void ksum_merge(KSum &a, const KSum &b) {
     two_sum_add(a, b.s);
     a.c += b.c;
 }

@@ -36,22 +36,31 @@ def java_sci(x):
 
 
 def java_double(x):
-    """Double.toString for the time column of ProjectedEnergyDensity."""
+    """Double.toString(x): the shortest digits that round-trip, plain decimal
+    for 1e-3 <= |x| < 1e7 (at least one fraction digit), otherwise
+    d.dddE<exp> with at least one fraction digit."""
     x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "-Infinity" if x < 0 else "Infinity"
     if x == 0.0:
-        return "0.0"
+        return "-0.0" if str(x).startswith("-") else "0.0"
+    sign, digits, exp = decimal.Decimal(repr(x)).as_tuple()
+    ds = "".join(str(v) for v in digits).lstrip("0") or "0"
+    # value = 0.ds * 10^(point), point = number of digits before the decimal point
+    point = len(digits) + exp - (len(digits) - len("".join(str(v) for v in digits).lstrip("0")))
+    ds = ds.rstrip("0") or "0"
+    neg = "-" if sign else ""
     ax = abs(x)
     if 1e-3 <= ax < 1e7:
-        r = repr(x)
-        return r if "." in r or "e" in r else r + ".0"
-    m, e = repr(x).split("e") if "e" in repr(x) else (None, None)
-    if m is None:
-        s = "%.17e" % x
-        m, e = s.split("e")
-        m = m.rstrip("0")
-    if "." not in m:
-        m += ".0"
-    return f"{m}E{int(e)}"
+        if point <= 0:
+            return neg + "0." + "0" * (-point) + ds
+        if point >= len(ds):
+            return neg + ds + "0" * (point - len(ds)) + ".0"
+        return neg + ds[:point] + "." + ds[point:]
+    frac = ds[1:] or "0"
+    return neg + ds[0] + "." + frac + "E" + str(point - 1)
 
 
 class Diagnostics:
@@ -154,6 +163,68 @@ class ProjectedEnergyDensity(Diagnostics):
                         f.write("\t".join(java_sci(v) for v in r) + "\n")
 
 
+class OccupationNumbersInTime(Diagnostics):
+    """diagnostics/methods/OccupationNumbersInTime.java: occupation numbers in
+    Coulomb gauge (SU(2)).  CSV output: a header with the grid size
+    (+ the momentum vectors for "csv_with_vectors"), then per measurement
+    "time, energy" and the occupation numbers (one line per colour when
+    colorful, else their colour sum); "csv_only_energy" writes the first line
+    only, "none" nothing.  The mirrored grid and cone windows are not provided."""
+
+    TYPES = ("csv", "csv_only_energy", "csv_with_vectors", "none")
+
+    def __init__(self, interval, output_type, path, colorful=False, max_iter=100, accuracy_goal=1e-18):
+        self.timeInterval = float(interval)
+        self.outputType = output_type
+        self.path = path
+        self.colorful = bool(colorful)
+        self.maxIter = int(max_iter)
+        self.accuracyGoal = float(accuracy_goal)
+        self.computationCounter = 0
+        self.occupationNumbers = None
+        self.energyDensity = None
+        if output_type not in self.TYPES:
+            raise ValueError(f"OccupationNumbersInTime: unsupported output type {output_type}")
+        if output_type != "none":
+            open(path, "w").close()
+
+    def initialize(self, s):
+        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        dims = s.grid.dims
+        if self.outputType == "none":
+            return
+        with open(self.path, "a") as f:
+            f.write(", ".join(str(int(d)) for d in dims) + "\n")
+            if self.outputType == "csv_with_vectors":
+                a = s.grid.getLatticeSpacing(0)
+                ks = []
+                for i in range(int(np.prod(dims))):
+                    pos = (i // (dims[1] * dims[2]), (i // dims[2]) % dims[1], i % dims[2])
+                    k = []
+                    for j in range(3):
+                        delta = pos[j] / float(dims[j])
+                        k.append(2.0 * delta * np.pi / a if delta < 0.5 else 2.0 * (delta - 1.0) * np.pi / a)
+                    ks.append(", ".join(java_double(v) for v in k))
+                f.write(", ".join(ks) + "\n")
+
+    def calculate(self, grid, particles, steps):
+        if steps % self.stepInterval != 0:
+            return
+        n, e, it, dv = grid.handle.occupation_numbers(self.maxIter, self.accuracyGoal,
+                                                      with_n=self.outputType != "csv_only_energy")
+        self.occupationNumbers, self.energyDensity = n, e
+        if self.outputType != "none":
+            with open(self.path, "a") as f:
+                f.write(java_double(self.computationCounter * self.timeInterval) + ", " + java_double(e) + "\n")
+                if self.outputType in ("csv", "csv_with_vectors"):
+                    if self.colorful:
+                        for k in range(n.shape[1]):
+                            f.write(", ".join(java_double(v) for v in n[:, k]) + "\n")
+                    else:
+                        f.write(", ".join(java_double(v) for v in n.sum(axis=1)) + "\n")
+        self.computationCounter += 1
+
+
 class TimeMeasurement(Diagnostics):
     """diagnostics/methods/TimeMeasurement.java: wall time per output interval."""
 
@@ -187,7 +258,12 @@ def from_yaml(out):
                                          o.get("computePoyntingVector", True)))
     for o in out.get("timeMeasurement") or []:
         ds.append(TimeMeasurement(o["path"], o["interval"]))
-    unsupported = set(out) - {"bulkQuantitiesInTime", "energyDensity", "projectedEnergyDensity", "timeMeasurement"}
+    for o in out.get("occupationNumbersInTime") or []:
+        if o.get("useMirroredGrid") is not None:
+            raise NotImplementedError("OccupationNumbersInTime: the mirrored grid and cone windows are not provided")
+        ds.append(OccupationNumbersInTime(o["interval"], o["outputType"], o["path"], bool(o.get("colorful", False))))
+    unsupported = set(out) - {"bulkQuantitiesInTime", "energyDensity", "projectedEnergyDensity", "timeMeasurement",
+                              "occupationNumbersInTime"}
     if unsupported:
         raise NotImplementedError(f"output generators not provided: {sorted(unsupported)}")
     return ds

@@ -1703,3 +1703,111 @@ void orc_super_jin(const orc_params *p, int ngroups, const int *orient, const lo
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Coulomb gauge and occupation numbers, SU(2) (physics/gauge/CoulombGauge.java, */
+/* physics/gauge/GaugeTransformation.java,                                    */
+/* diagnostics/methods/OccupationNumbersInTime.java)                          */
+/* ------------------------------------------------------------------------- */
+
+/* SU2GroupElement.getAlgebraElement (math/SU2GroupElement.java:234-252) */
+static void su2_log(const double *u, double *v)
+{
+    double norm = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+    norm = sqrt(norm);
+    if (norm < 1.E-15) {
+        v[0] = 2 * u[1]; v[1] = 2 * u[2]; v[2] = 2 * u[3];
+        return;
+    }
+    v[0] = 2.0 * asin(norm) / norm * u[1];
+    v[1] = 2.0 * asin(norm) / norm * u[2];
+    v[2] = 2.0 * asin(norm) / norm * u[3];
+}
+
+/* SU2AlgebraElement.getLink in the reference's own form (math/SU2AlgebraElement.java:140-152) */
+static void su2_link_ref(const double *v, double *u)
+{
+    double sum = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double mod = sqrt(sum) / 2;
+    double sinfakt = mod < 1.E-20 ? 0.0 : 0.5 / mod * sin(mod);
+    u[0] = cos(mod); u[1] = v[0] * sinfakt; u[2] = v[1] * sinfakt; u[3] = v[2] * sinfakt;
+}
+
+/* CoulombGauge.CalculateDivergence (:148-166) for every colour: div[c][x] =
+ * sum_dir A_c(U_dir(x)) - A_c(U_dir(x - dir)); returns the sum of squares in the
+ * reference's order (colour by colour, cells in sequence). */
+double orc_coulomb_divergence(const orc_params *p, const double *U, double *div)
+{
+    long V = vol(p);
+    double total = 0.0;
+    for (int c = 0; c < 3; c++) {
+        double s = 0.0;
+        for (long x = 0; x < V; x++) {
+            double d = 0.0;
+            for (int dir = 0; dir < 3; dir++) {
+                double a[3], b[3];
+                su2_log(link(p, U, x, dir), a);
+                su2_log(link(p, U, orc_shift(p, x, dir, -1), dir), b);
+                d += a[c] - b[c];
+            }
+            div[(size_t)c * V + x] = d;
+            s += d * d;
+        }
+        total += s;
+    }
+    return total;
+}
+
+/* g(x) = getLink(-psi(x)) (CoulombGauge.java:114-122) and GaugeTransformation's
+ * action (GaugeTransformation.java:57-90) on U, Unext and E.  psi: [3][V]. */
+void orc_coulomb_apply(const orc_params *p, const double *psi, double *U, double *Unext, double *E)
+{
+    long V = vol(p);
+    double *g = malloc(sizeof(double) * 4 * V);
+    for (long x = 0; x < V; x++) {
+        double v[3] = {psi[x] * -1, psi[V + x] * -1, psi[2 * V + x] * -1};
+        su2_link_ref(v, g + 4 * x);
+    }
+    for (long x = 0; x < V; x++)
+        for (int dir = 0; dir < 3; dir++) {
+            double gd[4], t[4], r[4];
+            long xs = orc_shift(p, x, dir, 1);
+            orc_group_adj(2, g + 4 * xs, gd);
+            double *u = U + ((size_t)x * 3 + dir) * 4;
+            orc_group_mult(2, g + 4 * x, u, t);
+            orc_group_mult(2, t, gd, r);
+            memcpy(u, r, sizeof(r));
+            u = Unext + ((size_t)x * 3 + dir) * 4;
+            orc_group_mult(2, g + 4 * x, u, t);
+            orc_group_mult(2, t, gd, r);
+            memcpy(u, r, sizeof(r));
+            /* E -> proj(g getLinearizedLink(E) g^dagger) (SU2AlgebraElement.java:133-138) */
+            double *e = E + ((size_t)x * 3 + dir) * 3;
+            double sum = (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) / 4;
+            double L[4] = {sqrt(1.0 - sum), e[0] / 2, e[1] / 2, e[2] / 2}, ga[4];
+            orc_group_adj(2, g + 4 * x, ga);
+            orc_group_mult(2, g + 4 * x, L, t);
+            orc_group_mult(2, t, ga, r);
+            orc_group_proj(2, r, e);
+        }
+    free(g);
+}
+
+/* The gauge field of OccupationNumbersInTime.calculate (:203-225):
+ * A[dir][c][x] = 0.5 (A_c(U_dir(x)) + A_c(Unext_dir(x))) * gainv and
+ * Ef[dir][c][x] = E_dir(x)_c * gainv. */
+void orc_occupation_fields(const orc_params *p, const double *U, const double *Unext, const double *E,
+                           double gainv, double *Ef, double *A)
+{
+    long V = vol(p);
+    for (long x = 0; x < V; x++)
+        for (int j = 0; j < 3; j++) {
+            double a0[3], a1[3];
+            su2_log(link(p, U, x, j), a0);
+            su2_log(link(p, Unext, x, j), a1);
+            for (int k = 0; k < 3; k++) {
+                Ef[((size_t)j * 3 + k) * V + x] = E[((size_t)x * 3 + j) * 3 + k] * gainv;
+                A[((size_t)j * 3 + k) * V + x] = 0.5 * (a0[k] * gainv + a1[k] * gainv);
+            }
+        }
+}

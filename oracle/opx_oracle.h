@@ -161,6 +161,12 @@ void orc_super_cin(const orc_params *p, int ngroups, const int *orient, const lo
 void orc_super_jin(const orc_params *p, int ngroups, const int *orient, const long *n, const long *base,
                    double *const *Q, int nthreads, long t, const double *Unext, double *J);
 
+/* ---- Coulomb gauge and occupation numbers (SU(2)) ---- */
+double orc_coulomb_divergence(const orc_params *p, const double *U, double *div);
+void orc_coulomb_apply(const orc_params *p, const double *psi, double *U, double *Unext, double *E);
+void orc_occupation_fields(const orc_params *p, const double *U, const double *Unext, const double *E,
+                           double gainv, double *Ef, double *A);
+
 #ifdef __cplusplus
 }
 #endif

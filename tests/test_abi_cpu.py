@@ -47,3 +47,12 @@ def test_invalid_config_rejected_before_device(native):
         with pytest.raises(N.OpixiError) as e:
             N.Handle(**kw)
         assert e.value.code == N.OPX_ERR_INVALID
+
+
+def test_java_double_format():
+    """Double.toString as documented in the Java SE API (plain decimal between
+    1e-3 and 1e7, otherwise computerized scientific notation)."""
+    from openpixi_gb300.diagnostics import java_double as j
+    assert j(100.0) == "100.0" and j(0.001) == "0.001" and j(1.0e-4) == "1.0E-4"
+    assert j(1.0e7) == "1.0E7" and j(9999999.0) == "9999999.0" and j(-3.5e-4) == "-3.5E-4"
+    assert j(0.0) == "0.0" and j(1.0 / 3.0) == "0.3333333333333333" and j(123456789.0) == "1.23456789E8"

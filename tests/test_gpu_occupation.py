@@ -1,0 +1,72 @@
+"""Coulomb gauge and occupation numbers (SU(2)) on the GPU against the oracle,
+through the C ABI: the reference's CoulombGaugeTest iteration counts, the
+occupation numbers within 1e-9 of the largest and the energy density within
+1e-10 (FFT rounding: cuFFT against numpy), the same number of Coulomb
+iterations, and the handle's fields untouched."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import openpixi_gb300 as opx
+from openpixi_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def gauge_transform(g, psi):
+    from oracle import lib, _p
+    L = lib()
+    L.orc_coulomb_apply.argtypes = [C.c_void_p] * 5
+    L.orc_coulomb_apply(g.pp, _p(np.ascontiguousarray(psi)), _p(g.U), _p(g.Unext), _p(g.E))
+
+
+def handle_of(g, precision=N.OPX_F64):
+    h = opx.Handle(2, g.dims, a=g.a, dt=g.dt, g=g.g, precision=precision)
+    h.upload(N.FIELD_U, g.U)
+    h.upload(N.FIELD_UNEXT, g.Unext)
+    h.upload(N.FIELD_E, g.E)
+    return h
+
+
+@pytest.mark.parametrize("f1,f2,expect", [((0, 0, 0), (0, 0, 0), 1), ((.1, 0, 0), (0, 0, 0), 2),
+                                          ((.1, 0, 0), (0, .1, 0), 3)])
+def test_coulomb_gauge_known_answers(native, orc, f1, f2, expect):
+    g = orc.OracleGrid(2, (2, 2, 2), dt=0.1)
+    psi = np.zeros((3, 8))
+    psi[:, 0] = -np.array(f1)
+    psi[:, 1] = -np.array(f2)
+    gauge_transform(g, psi)
+    h = handle_of(g)
+    _, _, it, dv = h.occupation_numbers(with_n=False)
+    assert dv < 1e-18
+    if expect < 3:
+        assert it == expect
+    else:
+        assert it > 2
+
+
+def test_occupation_numbers_vs_oracle(native, orc):
+    from oracle import occupation
+    g = orc.OracleGrid(2, (8, 6, 10), dt=0.05, g=1.3)
+    g.random_links(5, 0.15)
+    g.random_e(5, 0.1)
+    g.update_links()
+    n_ref, e_ref, conv = occupation.occupation_numbers(g)
+    h = handle_of(g)
+    U0 = h.download(N.FIELD_U)
+    n, e, it, dv = h.occupation_numbers()
+    assert it == len(conv)
+    assert np.abs(n - n_ref).max() <= 1e-9 * np.abs(n_ref).max()
+    assert abs(e - e_ref) <= 1e-10 * abs(e_ref)
+    assert np.array_equal(h.download(N.FIELD_U), U0)
+    # an FP32 handle measures in FP64 on widened copies of its fields
+    h32 = handle_of(g, precision=N.OPX_F32)
+    n32, e32, _, _ = h32.occupation_numbers()
+    assert abs(e32 - e_ref) <= 1e-5 * abs(e_ref)
+
+
+def test_occupation_rejects_su3(native):
+    h = opx.Handle(3, (4, 4, 4))
+    with pytest.raises(opx.OpixiError):
+        h.occupation_numbers()

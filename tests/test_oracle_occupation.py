@@ -1,0 +1,81 @@
+"""CPU checks of the Coulomb-gauge / occupation-number oracle (SU(2)).
+
+Pins: the reference's CoulombGaugeTest known answers (iteration counts on a
+2x2x2 lattice: a trivial configuration converges in 1 iteration, an abelian
+gauge transformation in exactly 2, a non-abelian one in more than 2, each to
+the accuracy goal), gauge invariance of the occupation numbers' input (the
+Coulomb-gauge result does not depend on a prior random gauge transformation
+beyond the residual), and the energy from the occupation numbers against the
+field energy for weak fields."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def occ(orc):
+    from oracle import occupation as m
+    return m
+
+
+def gauge_transform(orc, g, psi):
+    """GaugeTransformation with g(x) = getLink(-psi(x)) applied to U, Unext, E."""
+    from oracle import lib, _p
+    L = lib()
+    L.orc_coulomb_apply.argtypes = [C.c_void_p] * 5
+    L.orc_coulomb_apply(g.pp, _p(np.ascontiguousarray(psi)), _p(g.U), _p(g.Unext), _p(g.E))
+
+
+@pytest.mark.parametrize("f1,f2,expect", [((0, 0, 0), (0, 0, 0), "1"), ((.1, 0, 0), (0, 0, 0), "2"),
+                                          ((.1, 0, 0), (0, .1, 0), ">2")])
+def test_coulomb_gauge_known_answers(orc, occ, f1, f2, expect):
+    # CoulombGaugeTest.testForSU2Fields: 2x2x2 trivial field, g at sites 0 and 1
+    g = orc.OracleGrid(2, (2, 2, 2), dt=0.1)
+    psi = np.zeros((3, 8))
+    psi[:, 0] = -np.array(f1)
+    psi[:, 1] = -np.array(f2)
+    gauge_transform(orc, g, psi)
+    conv = occ.coulomb_gauge(g)
+    assert conv[-1] < 1e-18
+    if expect == "1":
+        assert len(conv) == 1
+    elif expect == "2":
+        assert len(conv) == 2
+    else:
+        assert len(conv) > 2
+
+
+def test_occupation_energy_weak_field(orc, occ):
+    """For weak fields the energy from the occupation numbers equals the
+    field energy 1/2 <E^2 + B^2> in physical units up to O(field^4) corrections."""
+    g = orc.OracleGrid(2, (8, 8, 8), dt=0.05)
+    g.random_links(5, 0.02)
+    g.random_e(5, 0.02)
+    g.gauss_project(tol_g2=1e-28)
+    sim = orc.OracleSimulation(g)
+    sim.initialize()
+    n, energy, conv = occ.occupation_numbers(g)
+    assert conv[-1] < 1e-18
+    b = g.bulk()
+    field_energy = 0.5 * (b[11] + b[12])
+    assert abs(energy - field_energy) <= 0.05 * field_energy, (energy, field_energy)
+    assert np.all(n.sum(axis=1) > -1e-12 * n.max())
+
+
+def test_occupation_gauge_invariant(orc, occ):
+    """A random gauge transformation before the measurement changes the
+    colour-summed occupation numbers and the energy only at the level of the
+    Coulomb-gauge residual (the Coulomb gauge leaves a global colour rotation,
+    which mixes the colour components)."""
+    g = orc.OracleGrid(2, (6, 6, 6), dt=0.05)
+    g.random_links(7, 0.1)
+    g.random_e(7, 0.1)
+    g.update_links()
+    n0, e0, _ = occ.occupation_numbers(g)
+    rng = np.random.default_rng(3)
+    gauge_transform(orc, g, rng.normal(0, 0.2, (3, g.V)))
+    n1, e1, _ = occ.occupation_numbers(g)
+    assert abs(e1 - e0) <= 1e-6 * e0
+    s0, s1 = n0.sum(axis=1), n1.sum(axis=1)
+    assert np.abs(s1 - s0).max() <= 1e-5 * np.abs(s0).max()
