@@ -129,6 +129,13 @@ int opx_set_evaluatable(opx_ctx *ctx, const uint8_t *mask, size_t count);
 int opx_step_links(opx_ctx *ctx);
 /* FieldSolver.step -> CombinedUpdate (FastTYMSolver.java:24-63) */
 int opx_update_grid(opx_ctx *ctx);
+/* Field solver of opx_update_grid / opx_step (Settings.applySimulationTypeSetting,
+ * physics/Settings.java:540-581): FastTYMSolver (the default), or
+ * ImplicitTYMSolver(implicitSolverIterations, implicitSolverDamping)
+ * (physics/fields/ImplicitTYMSolver.java:35-58; SU(2)) for the implicit CGC types. */
+#define OPX_SOLVER_FAST 0
+#define OPX_SOLVER_IMPLICIT 1
+int opx_set_field_solver(opx_ctx *ctx, int kind, int iterations, double damping);
 /* Grid.storeFields -> Cell.reassignLinks (Grid.java:591-593, Cell.java:173-177) */
 int opx_store_fields(opx_ctx *ctx);
 /* Simulation.initialize (Simulation.java:318-352) */

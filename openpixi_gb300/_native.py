@@ -24,6 +24,7 @@ OPX_F32 = 1
 FIELD_U, FIELD_UNEXT, FIELD_E, FIELD_J, FIELD_RHO = range(5)
 LAYOUT_REF, LAYOUT_GEN = 0, 1
 PHASE_EOM, PHASE_CPIC, PHASE_DIA, PHASE_LINKS = range(4)
+SOLVER_FAST, SOLVER_IMPLICIT = 0, 1
 NUM_PHASES = 4
 
 # Every symbol include/opixi.h declares (checked by the CPU test suite).
@@ -43,7 +44,7 @@ EXPORTED = [
     "opx_batch_kernel_launches",
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
     "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
-    "opx_super_download", "opx_super_upload", "opx_occupation_numbers",
+    "opx_super_download", "opx_super_upload", "opx_occupation_numbers", "opx_set_field_solver",
 ]
 
 
@@ -149,6 +150,7 @@ def load(path=None):
         "opx_super_download": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, C.c_size_t]),
         "opx_super_upload": (C.c_int, [vp, C.c_int, C.c_long, C.c_long, vp]),
         "opx_occupation_numbers": (C.c_int, [vp, C.c_int, C.c_double, vp, C.c_size_t, vp, vp, vp]),
+        "opx_set_field_solver": (C.c_int, [vp, C.c_int, C.c_int, C.c_double]),
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
         "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
@@ -334,6 +336,10 @@ class Handle:
                 setattr(arr[k], f, nu[f])
         self.check(self.L.opx_cgc_mv(self.h, arr, len(nuclei)))
         self.np = self.L.opx_particles_count(self.h)
+
+    def set_field_solver(self, kind, iterations=0, damping=0.0):
+        """FastTYMSolver (SOLVER_FAST) or ImplicitTYMSolver(iterations, damping) (SOLVER_IMPLICIT)."""
+        self.check(self.L.opx_set_field_solver(self.h, int(kind), int(iterations), float(damping)))
 
     def occupation_numbers(self, max_iter=100, accuracy_goal=1e-18, with_n=True):
         """OccupationNumbersInTime: (n [V][3] or None, energy density, iterations, last divergence)."""

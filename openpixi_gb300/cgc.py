@@ -65,12 +65,14 @@ class CGCInitialCondition:
 
     def applyInitialCondition(self, s):
         # the particle creator follows the simulation type (CGCInitialCondition.java:76-87)
-        if s.simulationType not in ("TemporalCGCNGP", "TemporalOptimizedCGCNGP"):
+        from .settings import SUPER_PARTICLES
+        if s.simulationType not in ("TemporalCGCNGP", "TemporalImplicitCGCNGP", "TemporalOptimizedCGCNGP",
+                                    "TemporalOptimizedImplicitCGCNGP"):
             raise RuntimeError("CGCInitialCondition: simulation type not supported!")
         if self.computeTadpole or self.computeDipole:
             raise NotImplementedError("Wilson line observables (tadpole, dipole) are not provided")
         h = s.grid.handle
-        if s.simulationType == "TemporalOptimizedCGCNGP":
+        if s.simulationType in SUPER_PARTICLES:
             # LightConeNGPSuperParticleCreator: CGCSuperParticle groups
             h.cgc_mv_super([self.initialChargeDensity.as_nucleus()])
             s.particles = h.super_groups

@@ -67,7 +67,8 @@ static void fill_identity(Ctx &c, void *U) {
 static void release(Ctx &c) {
     cpic_free(c);
     super_free(c);
-    void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.status};
+    void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.status,
+                   c.imp_Ua, c.imp_Ub, c.imp_E};
     for (void *p : dev) if (p) cudaFree(p);
     if (c.red_host) cudaFreeHost(c.red_host);
     if (c.status_host) cudaFreeHost(c.status_host);
@@ -289,7 +290,12 @@ int opx_update_grid(opx_ctx *ctx) {
     API_CHECK(ctx);
     Ctx &c = ctx->c;
     phase_begin(c);
-    launch_update_grid(c, false);
+    if (c.imp_solver) {
+        int rc = launch_implicit_update(c);
+        if (rc) return rc;
+    } else {
+        launch_update_grid(c, false);
+    }
     phase_end(c, OPX_PHASE_EOM);
     return check_launch(c, "opx_update_grid");
 }
@@ -346,7 +352,12 @@ static int one_step(Ctx &c) {
     std::swap(c.U, c.Unext);  // storeFields
     const bool reunit = c.prec == OPX_F32 && c.cfg.reunit_every > 0 && (c.steps % c.cfg.reunit_every) == 0;
     phase_begin(c);
-    launch_update_grid(c, reunit);
+    if (c.imp_solver) {
+        int rc = launch_implicit_update(c);
+        if (rc) return rc;
+    } else {
+        launch_update_grid(c, reunit);
+    }
     phase_end(c, OPX_PHASE_EOM);
     if (c.P.n > 0) {
         phase_begin(c);
@@ -364,8 +375,26 @@ int opx_step(opx_ctx *ctx, int nsteps) {
     API_CHECK(ctx);
     Ctx &c = ctx->c;
     if (nsteps < 0) { c.err = "opx_step: nsteps < 0"; return OPX_ERR_INVALID; }
-    for (int k = 0; k < nsteps; k++) one_step(c);
+    for (int k = 0; k < nsteps; k++) {
+        int rc = one_step(c);
+        if (rc) return rc;
+    }
     return check_launch(c, "opx_step");
+}
+
+int opx_set_field_solver(opx_ctx *ctx, int kind, int iterations, double damping) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (kind == OPX_SOLVER_FAST) { c.imp_solver = false; return OPX_OK; }
+    if (kind != OPX_SOLVER_IMPLICIT || iterations < 0 || !(damping >= 0 && damping <= 1)) {
+        c.err = "opx_set_field_solver: kind FAST or IMPLICIT, iterations >= 0, 0 <= damping <= 1";
+        return OPX_ERR_INVALID;
+    }
+    if (c.nc != 2) { c.err = "opx_set_field_solver: the implicit solver is provided for SU(2)"; return OPX_ERR_UNSUPPORTED; }
+    c.imp_solver = true;
+    c.imp_iterations = iterations;
+    c.imp_damping = damping;
+    return OPX_OK;
 }
 
 int opx_synchronize(opx_ctx *ctx) {

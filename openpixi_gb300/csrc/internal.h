@@ -66,6 +66,11 @@ struct Ctx {
     long steps = 0;
     long launches = 0;
     Particles P;
+    // field solver: FastTYMSolver (imp_solver false) or ImplicitTYMSolver
+    bool imp_solver = false;
+    int imp_iterations = 0;
+    double imp_damping = 0.0;
+    void *imp_Ua = nullptr, *imp_Ub = nullptr, *imp_E = nullptr;  // the implicit grid's links and E
     std::vector<SuperGroup> sg;  // super-particle groups in list order
     int sg_ppc = 0;
     bool profiling = false;
@@ -77,6 +82,7 @@ struct Ctx {
 
 // ---- launchers (field_kernels.cu) ----
 void launch_update_grid(Ctx &c, bool reunit);
+int launch_implicit_update(Ctx &c);  // ImplicitTYMSolver.step in place of launch_update_grid
 void launch_update_links(Ctx &c);
 void launch_reunit(Ctx &c, void *links);
 // ---- reductions (reduce_kernels.cu) ----

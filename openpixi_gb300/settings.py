@@ -20,7 +20,10 @@ SIMULATION_TYPES = {
 }
 # simulation types whose solver/interpolator combination this library provides
 # (Settings.applySimulationTypeSetting, physics/Settings.java:540-581)
-SUPPORTED = {"TemporalYangMills", "TemporalCGCNGP", "TemporalOptimizedCGCNGP"}
+SUPPORTED = {"TemporalYangMills", "TemporalCGCNGP", "TemporalOptimizedCGCNGP", "TemporalImplicitCGCNGP",
+             "TemporalOptimizedImplicitCGCNGP"}
+IMPLICIT = {"TemporalImplicitCGCNGP", "TemporalOptimizedImplicitCGCNGP"}
+SUPER_PARTICLES = {"TemporalOptimizedCGCNGP", "TemporalOptimizedImplicitCGCNGP"}
 
 
 class Settings:
@@ -51,6 +54,9 @@ class Settings:
         self.precision = "f64"
         self.reunitarizeEvery = 0
         self.device = 0
+        # ImplicitTYMSolver parameters (Settings.java:79-80)
+        self.implicitSolverIterations = 0
+        self.implicitSolverDamping = 0.0
 
     # ---- accessors named as in Settings.java ----
     def setSimulationType(self, t):
@@ -152,6 +158,11 @@ def apply_yaml(doc, settings=None):
         s.setCouplingConstant(doc["couplingConstant"])
     if doc.get("numberOfThreads") is not None:
         s.setNumOfThreads(doc["numberOfThreads"])
+    # YamlSettings.java:29-30, 100-105
+    if doc.get("implicitSolverIterations") is not None:
+        s.implicitSolverIterations = int(doc["implicitSolverIterations"])
+    if doc.get("implicitSolverDamping") is not None:
+        s.implicitSolverDamping = float(doc["implicitSolverDamping"])
     nd = s.numberOfDimensions
     if doc.get("gridSteps") is not None:
         if len(doc["gridSteps"]) != nd:

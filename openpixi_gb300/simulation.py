@@ -46,6 +46,18 @@ class FastTYMSolver(FieldSolver):
         grid._dirty()
 
 
+class ImplicitTYMSolver(FastTYMSolver):
+    """physics/fields/ImplicitTYMSolver.java: the implicit update runs on the device
+    (opx_set_field_solver with OPX_SOLVER_IMPLICIT); stepLinks is FastTYMSolver's."""
+
+    def __init__(self, implicitIterations=0, implicitDampingFactor=0.0):
+        self.implicitIterations = int(implicitIterations)
+        self.implicitDampingFactor = float(implicitDampingFactor)
+
+    def clone(self):
+        return ImplicitTYMSolver(self.implicitIterations, self.implicitDampingFactor)
+
+
 class Grid:
     def __init__(self, settings):
         prec = N.OPX_F32 if settings.precision == "f32" else N.OPX_F64
@@ -60,7 +72,13 @@ class Grid:
         self.g = settings.couplingConstant
         self.handle = N.Handle(self.numCol, self.dims, a=self.a, dt=self.at, g=self.g, precision=prec,
                                reunit_every=settings.reunitarizeEvery, device=settings.device)
-        self.fsolver = FastTYMSolver()
+        from .settings import IMPLICIT
+        if settings.simulationType in IMPLICIT:
+            self.fsolver = ImplicitTYMSolver(settings.implicitSolverIterations, settings.implicitSolverDamping)
+            self.handle.set_field_solver(N.SOLVER_IMPLICIT, settings.implicitSolverIterations,
+                                         settings.implicitSolverDamping)
+        else:
+            self.fsolver = FastTYMSolver()
         self.V = int(np.prod(self.dims))
         self._cache = {}
         self.simulationSteps = 0
@@ -255,7 +273,8 @@ class Simulation:
         if not self.particles:
             return None
         h = self.grid.handle
-        if self.simulationType == "TemporalOptimizedCGCNGP":
+        from .settings import SUPER_PARTICLES
+        if self.simulationType in SUPER_PARTICLES:
             return [h.super_download(k) for k in range(h.super_groups)]
         return h.particles_download()
 

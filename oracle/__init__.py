@@ -196,6 +196,13 @@ class OracleGrid:
     def update_grid(self):
         lib().orc_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext), _p(self.active))
 
+    def update_grid_implicit(self, iterations, damping):
+        """ImplicitTYMSolver.step (SU(2)) in place of update_grid."""
+        rc = lib().orc_implicit_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),
+                                            _p(self.active), int(iterations), C.c_double(damping))
+        if rc != 0:
+            raise ValueError("implicit solver: SU(2) only")
+
     def update_grid_omp(self, nthreads):
         lib().orc_update_grid_omp(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),
                                   _p(self.active), int(nthreads))
@@ -306,10 +313,11 @@ class OracleParticles:
 class OracleSimulation:
     """Phase order of physics/Simulation.java (initialize :318-352, step :373-435)."""
 
-    def __init__(self, grid, particles=None):
+    def __init__(self, grid, particles=None, implicit=None):
         self.grid = grid
         self.particles = particles
         self.steps = 0
+        self.implicit = implicit  # (iterations, damping) for ImplicitTYMSolver
 
     def _cpic_phases(self):
         g, P, L = self.grid, self.particles, lib()
@@ -340,5 +348,8 @@ class OracleSimulation:
         if P is not None and P.n:
             lib().orc_cpic_reassign(self.grid.nc, C.c_long(P.n), _p(P.pos0), _p(P.pos1), _p(P.Q0), _p(P.Q1))
         self.grid.store_fields()
-        self.grid.update_grid()
+        if self.implicit is not None:
+            self.grid.update_grid_implicit(*self.implicit)
+        else:
+            self.grid.update_grid()
         self._cpic_phases()

@@ -167,11 +167,12 @@ class OracleSuperSimulation:
     optimized CGC type: field update, then CGCSuperParticleInterpolationNGP's
     charge density and current (the particle solver does nothing)."""
 
-    def __init__(self, grid, groups, nthreads=1):
+    def __init__(self, grid, groups, nthreads=1, implicit=None):
         self.grid = grid
         self.groups = groups
         self.nthreads = nthreads
         self.steps = 0
+        self.implicit = implicit  # (iterations, damping) for ImplicitTYMSolver
 
     def _args(self):
         k = len(self.groups)
@@ -200,7 +201,10 @@ class OracleSuperSimulation:
     def step(self):
         self.steps += 1
         self.grid.store_fields()
-        self.grid.update_grid()
+        if self.implicit is not None:
+            self.grid.update_grid_implicit(*self.implicit)
+        else:
+            self.grid.update_grid()
         self._phases(self.steps)
 
 

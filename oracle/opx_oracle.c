@@ -1811,3 +1811,132 @@ void orc_occupation_fields(const orc_params *p, const double *U, const double *U
             }
         }
 }
+
+/* ------------------------------------------------------------------------- */
+/* ImplicitTYMSolver.step (physics/fields/ImplicitTYMSolver.java:35-58), SU(2) */
+/* ------------------------------------------------------------------------- */
+
+/* SU2GroupElement.pow(x) = getAlgebraElement().mult(x).getLink() (math/SU2GroupElement.java:269-271) */
+static void su2_pow(const double *u, double x, double *out)
+{
+    double v[3];
+    su2_log(u, v);
+    for (int c = 0; c < 3; c++) v[c] = v[c] * x;
+    su2_link_ref(v, out);
+}
+
+/* ImplicitStep.getPlaquetteSum (:136-177): plaquettes closed along the central
+ * link, with the links of direction i / d taken at time -1 (W_m, the grid's
+ * Unext slot, which holds the previous U), 0 (W_0 = grid U) or +1 (W_p = the
+ * implicit grid's U), implicit time in the transverse plane and along the beam. */
+static void implicit_plaquette_sum(const orc_params *p, const double *Wm, const double *W0, const double *Wp,
+                                   long index, int d, int beam, int time, double *S)
+{
+    const int ng = 4;
+    memset(S, 0, sizeof(double) * ng);
+    long ci1 = orc_shift(p, index, d, 1);
+    for (int i = 0; i < 3; i++) {
+        if (i == d) continue;
+        int inT = (i != beam) && (d != beam);
+        int td = 0, ti = 0;
+        if (inT) { td = time; ti = time; }
+        else { if (d == beam) td = time; else if (i == beam) ti = time; }
+        const double *Wd = td < 0 ? Wm : (td > 0 ? Wp : W0);
+        const double *Wi = ti < 0 ? Wm : (ti > 0 ? Wp : W0);
+        long ci2 = orc_shift(p, index, i, 1), ci3 = orc_shift(p, ci1, i, -1), ci4 = orc_shift(p, index, i, -1);
+        double U1[4], U2[4], t[4], adj[4];
+        orc_group_adj(2, link(p, Wd, ci2, d), adj);
+        orc_group_mult(2, link(p, Wi, ci1, i), adj, U1);
+        orc_group_adj(2, link(p, Wi, index, i), adj);
+        orc_group_mult(2, U1, adj, t);
+        memcpy(U1, t, sizeof(t));
+        orc_group_mult(2, link(p, Wd, ci4, d), link(p, Wi, ci3, i), U2);
+        orc_group_adj(2, U2, t);
+        orc_group_mult(2, t, link(p, Wi, ci4, i), U2);
+        double areaFactor = 1.0 / pow(p->a[i], 2);
+        for (int k = 0; k < ng; k++) U1[k] = U1[k] + U2[k];
+        orc_group_mult(2, link(p, Wd, index, d), U1, t);
+        for (int k = 0; k < ng; k++) U1[k] = t[k] * areaFactor;
+        for (int k = 0; k < ng; k++) S[k] = S[k] + U1[k];
+    }
+}
+
+/* In place of orc_update_grid for the implicit solver: U current links, Unext
+ * the previous links (the slot after storeFields), E, J; writes E and Unext of
+ * the active cells.  Returns -1 for SU(3). */
+int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, const double *J, double *Unext,
+                             const uint8_t *active, int iterations, double damping)
+{
+    if (p->nc != 2) return -1;
+    const int ng = 4, na = 3, beam = 0;
+    long V = vol(p);
+    size_t nl = (size_t)V * 3 * ng, ne = (size_t)V * 3 * na;
+    /* Grid(grid): the implicit grid is a copy */
+    double *Ui = malloc(sizeof(double) * nl), *Uin = malloc(sizeof(double) * nl), *Ei = malloc(sizeof(double) * ne);
+    memcpy(Ui, U, sizeof(double) * nl);
+    memcpy(Uin, Unext, sizeof(double) * nl);
+    memcpy(Ei, E, sizeof(double) * ne);
+    /* ImplicitBegin (:68-90) */
+    for (long x = 0; x < V; x++) {
+        if (active && !active[x]) continue;
+        for (int i = 0; i < 3; i++) {
+            double S[4], temp[4], pr[3], ve[3], Vl[4], t[4];
+            double unitFactor = -(p->g * p->a[i]) * p->dt;
+            orc_staple_sum(p, U, x, i, S);
+            orc_group_mult(2, link(p, U, x, i), S, temp);
+            orc_group_proj(2, temp, pr);
+            double *e = Ei + ((size_t)x * 3 + i) * na;
+            const double *j = J + ((size_t)x * 3 + i) * na;
+            for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * p->dt;
+            for (int c = 0; c < na; c++) e[c] = e[c] + j[c] * unitFactor;
+            for (int c = 0; c < na; c++) ve[c] = e[c] * -p->dt;
+            orc_alg_getlink(2, ve, Vl);
+            orc_group_mult(2, Vl, link(p, U, x, i), t);
+            memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+        }
+    }
+    for (int it = 0; it < iterations; it++) {
+        double *sw = Ui; Ui = Uin; Uin = sw; /* implicitGrid.storeFields() */
+        /* ImplicitStep (:103-131) */
+        for (long x = 0; x < V; x++) {
+            if (active && !active[x]) continue;
+            for (int i = 0; i < 3; i++) {
+                double S[4], pr[3], ve[3], Vl[4], t[4];
+                double unitFactor = -(p->g * p->a[i]) * p->dt;
+                double *e = Ei + ((size_t)x * 3 + i) * na;
+                const double *j = J + ((size_t)x * 3 + i) * na;
+                memcpy(e, E + ((size_t)x * 3 + i) * na, sizeof(double) * na);
+                implicit_plaquette_sum(p, Unext, U, Ui, x, i, beam, +1, S);
+                orc_group_proj(2, S, pr);
+                for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * (p->dt * 0.5);
+                implicit_plaquette_sum(p, Unext, U, Ui, x, i, beam, -1, S);
+                orc_group_proj(2, S, pr);
+                for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * (p->dt * 0.5);
+                for (int c = 0; c < na; c++) e[c] = e[c] + j[c] * unitFactor;
+                for (int c = 0; c < na; c++) ve[c] = e[c] * -p->dt;
+                orc_alg_getlink(2, ve, Vl);
+                orc_group_mult(2, Vl, link(p, U, x, i), t);
+                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+            }
+        }
+        /* ImplicitDamping (:195-207) */
+        for (long x = 0; x < V; x++) {
+            if (active && !active[x]) continue;
+            for (int i = 0; i < 3; i++) {
+                double U1[4], U2[4], t[4];
+                su2_pow(Uin + ((size_t)x * 3 + i) * ng, 1 - damping, U1);
+                su2_pow(Ui + ((size_t)x * 3 + i) * ng, damping, U2);
+                orc_group_mult(2, U2, U1, t);
+                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+            }
+        }
+    }
+    /* ImplicitEnd (:217-226) */
+    for (long x = 0; x < V; x++) {
+        if (active && !active[x]) continue;
+        memcpy(E + (size_t)x * 3 * na, Ei + (size_t)x * 3 * na, sizeof(double) * 3 * na);
+        memcpy(Unext + (size_t)x * 3 * ng, Uin + (size_t)x * 3 * ng, sizeof(double) * 3 * ng);
+    }
+    free(Ui); free(Uin); free(Ei);
+    return 0;
+}

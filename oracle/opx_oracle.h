@@ -167,6 +167,10 @@ void orc_coulomb_apply(const orc_params *p, const double *psi, double *U, double
 void orc_occupation_fields(const orc_params *p, const double *U, const double *Unext, const double *E,
                            double gainv, double *Ef, double *A);
 
+/* ---- ImplicitTYMSolver.step (SU(2); -1 for SU(3)) ---- */
+int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, const double *J, double *Unext,
+                             const uint8_t *active, int iterations, double damping);
+
 #ifdef __cplusplus
 }
 #endif

@@ -334,3 +334,32 @@ def test_poynting_rows_against_independent_matrices(orc):
         got = g.projected_poynting(d)
         assert np.allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max()), (d, got, ref)
         assert np.abs(ref).max() > 1e-4
+
+
+def test_implicit_solver_properties(orc):
+    """ImplicitTYMSolver (physics/fields/ImplicitTYMSolver.java): with no
+    iterations it is the explicit FastTYMSolver update bit for bit (ImplicitBegin
+    is the CombinedUpdate); with iterations and no damping the fixed-point
+    iteration converges (successive iterates approach each other)."""
+    g = orc.OracleGrid(2, (6, 6, 6), dt=0.05)
+    g.random_links(3, 0.3)
+    g.random_e(3, 0.3)
+    g.gauss_project()
+    a, b = g.copy(), g.copy()
+    sa = orc.OracleSimulation(a)
+    sb = orc.OracleSimulation(b, implicit=(0, 0.0))
+    sa.initialize()
+    sb.initialize()
+    for _ in range(4):
+        sa.step()
+        sb.step()
+    assert np.array_equal(a.U.view(np.uint64), b.U.view(np.uint64))
+    assert np.array_equal(a.E.view(np.uint64), b.E.view(np.uint64))
+    diffs = []
+    for it in (4, 8, 12):
+        c = g.copy()
+        sc = orc.OracleSimulation(c, implicit=(it, 0.0))
+        sc.initialize()
+        sc.step()
+        diffs.append(c.Unext.copy())
+    assert np.abs(diffs[2] - diffs[1]).max() < np.abs(diffs[1] - diffs[0]).max()
