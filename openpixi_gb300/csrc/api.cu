@@ -112,7 +112,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     c.na = c.nc == 3 ? 8 : 3;
     c.na_ref = c.nc == 3 ? 9 : 3;
     c.prec = cfg->precision;
-    c.pair_kernel = std::getenv("OPX_SU3_SCALAR") == nullptr;
+    c.pair_kernel = std::getenv("OPX_ONE_SITE_FP32") == nullptr;
     c.rsize = c.prec == OPX_F64 ? 8 : 4;
     bool ok = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) == cudaSuccess;
     auto al = [&](void **p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) { ok = false; *p = nullptr; } };

@@ -52,8 +52,9 @@ struct Ctx {
     void *U = nullptr, *Unext = nullptr, *E = nullptr, *J = nullptr, *rho = nullptr;
     uint8_t *active = nullptr, *eval = nullptr;  // null = all true
     bool j_nonzero = false;
-    // SU(3) FP32 leapfrog with two sites per thread in paired FP32 instructions
-    // (environment OPX_SU3_SCALAR=1 selects the one-site-per-thread form)
+    // SU(3) FP32 leapfrog and reduction with two sites per thread in paired FP32
+    // instructions (environment OPX_ONE_SITE_FP32=1 selects the
+    // one-site-per-thread forms)
     bool pair_kernel = true;
     double *staging = nullptr;
     size_t staging_len = 0;  // doubles

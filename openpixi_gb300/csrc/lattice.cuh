@@ -128,6 +128,30 @@ __device__ __forceinline__ long shift_d(const Lat &L, long s, int xd, int d, int
     return xd == 0 ? s + (long)(nd - 1) * st : s - st;
 }
 __device__ __forceinline__ int pick(int a0, int a1, int a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
+template <typename T> __device__ __forceinline__ T pick3(T a0, T a1, T a2, int d) {
+    return d == 0 ? a0 : (d == 1 ? a1 : a2);
+}
+
+// Periodic neighbour offsets of a site, computed once: s + f_d is x + d,
+// s + b_d is x - d; and x + i - j is s + f_i + b_j for i != j (the j
+// coordinate of x + i is that of x).
+template <typename I> struct Deltas {
+    I f0, f1, f2, b0, b1, b2;
+    __device__ __forceinline__ I f(int d) const { return pick3(f0, f1, f2, d); }
+    __device__ __forceinline__ I b(int d) const { return pick3(b0, b1, b2, d); }
+};
+template <typename I> __device__ __forceinline__ Deltas<I> deltas(const Lat &L, const int *x) {
+    Deltas<I> D;
+    const I st0 = (I)L.stride[0], st1 = (I)L.stride[1];
+    const I w0 = (I)(L.n[0] - 1) * st0, w1 = (I)(L.n[1] - 1) * st1, w2 = (I)(L.n[2] - 1);
+    D.f0 = x[0] == L.n[0] - 1 ? -w0 : st0;
+    D.b0 = x[0] == 0 ? w0 : -st0;
+    D.f1 = x[1] == L.n[1] - 1 ? -w1 : st1;
+    D.b1 = x[1] == 0 ? w1 : -st1;
+    D.f2 = x[2] == L.n[2] - 1 ? -w2 : (I)1;
+    D.b2 = x[2] == 0 ? w2 : (I)-1;
+    return D;
+}
 __device__ __forceinline__ double pickd(double a0, double a1, double a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
 
 // Read-only loads through the non-coherent cache for built-in element types;

@@ -24,7 +24,7 @@ __device__ __forceinline__ void update_site(const R *__restrict__ U, R *__restri
     constexpr int NA = G::NA;
     int x[3];
     site_coords(L, s, x);
-    const int x0 = x[0], x1 = x[1], x2 = x[2];
+    const Deltas<long> D = deltas<long>(L, x);
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
     const LinkPlanes<G, R> Un{Unext, L.V};
     const AlgPlanes<NA, R> Ep{E, L.V};
@@ -33,16 +33,15 @@ __device__ __forceinline__ void update_site(const R *__restrict__ U, R *__restri
 
 #pragma unroll 1
     for (int i = 0; i < 3; i++) {
-        const int xi = pick(x0, x1, x2, i);
-        const long s_pi = shift_d(L, s, xi, i, +1);  // x + i
+        const long s_pi = s + D.f(i);  // x + i
         M S = G::zero();
 #pragma unroll 1
         for (int jj = 1; jj < 3; jj++) {
             const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
-            const int xj = pick(x0, x1, x2, j);
-            const long s_pj = shift_d(L, s, xj, j, +1);       // x + j
-            const long s_mj = shift_d(L, s, xj, j, -1);       // x - j
-            const long s_pimj = shift_d(L, s_pi, xj, j, -1);  // x + i - j
+            const long bj = D.b(j);
+            const long s_pj = s + D.f(j);  // x + j
+            const long s_mj = s + bj;      // x - j
+            const long s_pimj = s_pi + bj; // x + i - j
             // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
             M F = G::mul_adj(G::mul_adj(Up.load(j, s_pi), Up.load(i, s_pj)), Up.load(j, s));
             // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)

@@ -439,27 +439,27 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
     int xa[3], xb[3];
     coords<I>(L, sa, xa);
     coords<I>(L, sb, xb);
+    const Deltas<I> Da = deltas<I>(L, xa), Db = deltas<I>(L, xb);
     const P dt = bc(L.dtf), mdt = bc(-L.dtf);
 #pragma unroll 1
     for (int i = 0; i < 3; i++) {
-        const int xia = pick(xa[0], xa[1], xa[2], i), xib = pick(xb[0], xb[1], xb[2], i);
-        const I pia = shift<I>(L, sa, xia, i, +1), pib = shift<I>(L, sb, xib, i, +1);  // x + i
+        const I pia = sa + Da.f(i), pib = sb + Db.f(i);  // x + i
         M S = mzero();
 #pragma unroll 1
         for (int jj = 1; jj < 3; jj++) {
             const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
-            const int xja = pick(xa[0], xa[1], xa[2], j), xjb = pick(xb[0], xb[1], xb[2], j);
             const P f = bc(LatR<float>::inva2(L, j));
             {
                 // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
-                const I pja = shift<I>(L, sa, xja, j, +1), pjb = shift<I>(L, sb, xjb, j, +1);
+                const I pja = sa + Da.f(j), pjb = sb + Db.f(j);
                 const M T = mul_adj(load<I>(U, nblk, j, pia, pib), load<I>(U, nblk, i, pja, pjb));
                 acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
             }
             {
                 // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
-                const I mja = shift<I>(L, sa, xja, j, -1), mjb = shift<I>(L, sb, xjb, j, -1);
-                const I pimja = shift<I>(L, pia, xja, j, -1), pimjb = shift<I>(L, pib, xjb, j, -1);
+                const I bja = Da.b(j), bjb = Db.b(j);
+                const I mja = sa + bja, mjb = sb + bjb;
+                const I pimja = pia + bja, pimjb = pib + bjb;
                 const M C = mul(load<I>(U, nblk, i, mja, mjb), load<I>(U, nblk, j, pimja, pimjb));
                 acc_adj_mul(S, f, C, load<I>(U, nblk, j, mja, mjb));
             }

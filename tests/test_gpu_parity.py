@@ -201,11 +201,11 @@ def test_errors_are_status_codes(native):
 def _handle_env(g, scalar, **kw):
     import os
     if scalar:
-        os.environ["OPX_SU3_SCALAR"] = "1"
+        os.environ["OPX_ONE_SITE_FP32"] = "1"
     try:
         return handle_from_oracle(g, **kw)
     finally:
-        os.environ.pop("OPX_SU3_SCALAR", None)
+        os.environ.pop("OPX_ONE_SITE_FP32", None)
 
 
 @pytest.mark.parametrize("dims,masked", [((16, 16, 16), False), ((7, 9, 11), True), ((5, 6, 33), False)])
