@@ -279,3 +279,37 @@ def test_projected_poynting_matches_oracle(native, orc):
     h3 = opx.Handle(3, (4, 4, 4))
     with pytest.raises(opx.OpixiError):
         h3.projected_poynting(0)
+
+
+@pytest.mark.parametrize("nc,dims", [(2, (1, 8, 8)), (2, (2, 1, 16)), (3, (3, 4, 1)), (2, (1, 1, 1))])
+def test_degenerate_lattices(native, orc, nc, dims):
+    """Directions with one or two cells (the periodic neighbour is the cell
+    itself or its only other cell): FP64 leapfrog and reductions against the oracle."""
+    g = fresh(oracle_ic(nc, dims, 17, 0.3, 0.3))
+    h = handle_from_oracle(g)
+    sim = orc.OracleSimulation(g)
+    sim.initialize()
+    h.initialize()
+    for _ in range(5):
+        sim.step()
+        h.step(1)
+    assert link_rel_err(h.download(N.FIELD_U), g.U) <= 1e-10
+    assert field_rel_err(h.download(N.FIELD_E), g.E) <= 1e-10
+    assert np.allclose(bulk_vec(h.reduce()), g.bulk()[:11], rtol=1e-10, atol=1e-14)
+
+
+def test_empty_particle_list_and_oversized_lattice(native):
+    """An empty particle list gives zero charge and current; a lattice beyond
+    the 32-bit particle-cell keys is refused with a status code and the device
+    stays usable."""
+    h = opx.Handle(2, (8, 8, 8), dt=0.5)
+    z3 = np.zeros((0, 3))
+    h.particles_upload(z3, z3, z3, z3, z3, np.zeros(0, np.int32))
+    h.initialize()
+    h.step(2)
+    assert np.all(h.download(N.FIELD_RHO) == 0) and np.all(h.download(N.FIELD_J) == 0)
+    with pytest.raises(opx.OpixiError) as err:
+        opx.Handle(3, (4096, 4096, 2048), precision=N.OPX_F64)
+    assert err.value.code in (N.OPX_ERR_INVALID, N.OPX_ERR_NOMEM)
+    h2 = opx.Handle(2, (8, 8, 8))  # the device is still usable
+    h2.initialize()
