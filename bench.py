@@ -438,6 +438,127 @@ def bench_cgc(device, nsteps=300, oracle_steps=2):
     return out
 
 
+def bench_differentiation(device, ndir=64):
+    """Differentiation form: SU(2), 64^3, dt = 0.05, 200 steps, FP32 forward with
+    FP64 checkpoints every 14 steps, objective the mean energy density over the
+    central 16^3; the gradient w.r.t. the initial E checked on 64 seeded random
+    directions against central differences (h = 1e-4) of FP64 forward runs and
+    against the FP64 tangent-linear run."""
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    dims, nsteps, ckpt = (64, 64, 64), 200, 14
+    lo, hi = (24, 24, 24), (39, 39, 39)
+    h64 = opx.Handle(2, dims, dt=0.05, precision=N.OPX_F64, device=device)
+    h64.init_random(SEED + 5, 0.1, 0.1)
+    h64.gauss_project(1e-24)
+    h32 = opx.Handle(2, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
+    h32.upload(N.FIELD_U, h64.download(N.FIELD_U))
+    h32.upload(N.FIELD_E, h64.download(N.FIELD_E))
+    h32.synchronize()
+    t = time.perf_counter()
+    J32, g32 = h32.energy_gradient(nsteps, ckpt, lo, hi)
+    t32 = time.perf_counter() - t
+    t = time.perf_counter()
+    J64, g64 = h64.energy_gradient(nsteps, ckpt, lo, hi)
+    t64 = time.perf_counter() - t
+    rng = np.random.default_rng(64)
+    worst = {"fd": 0.0, "tl": 0.0, "f32_vs_tl": 0.0}
+    t = time.perf_counter()
+    for _ in range(ndir):
+        d = rng.normal(size=g64.shape)
+        adj = float((g64 * d).sum())
+        eps = 1e-4
+        fd = (h64.energy_objective(nsteps, lo, hi, d, eps) - h64.energy_objective(nsteps, lo, hi, d, -eps)) / (2 * eps)
+        _, dJ = h64.energy_tangent(nsteps, d, lo, hi)
+        worst["fd"] = max(worst["fd"], abs(fd - adj) / abs(adj))
+        worst["tl"] = max(worst["tl"], abs(adj - dJ) / abs(dJ))
+        worst["f32_vs_tl"] = max(worst["f32_vs_tl"], abs(float((g32 * d).sum()) - dJ) / abs(dJ))
+    tcheck = time.perf_counter() - t
+    h64.close()
+    h32.close()
+    return {"workload": "SU(2) 64^3, 200 steps, dt=0.05, ckpt 14, central 16^3 energy density",
+            "J": J64, "gradient_s_fp32_forward": t32, "gradient_s_fp64_forward": t64,
+            "directions": ndir, "worst_rel_vs_central_fd": worst["fd"], "worst_rel_vs_tangent_linear": worst["tl"],
+            "worst_rel_fp32_forward_vs_tangent_linear": worst["f32_vs_tl"], "check_s": tcheck,
+            "bars": {"fd": 1e-5, "tl": 1e-9, "f32": 1e-3}}
+
+
+def bench_configs(device):
+    """Parity of the other single-GPU configurations at full size:
+    SU(2) FP64 32^3, 100 steps (config 1) against the oracle per link; the SU(3)
+    FP32 form against the FP64 GPU run on 128^3 x 500 steps (energy and per
+    link) and against the oracle on a 32^3 lattice of the same generator."""
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    import oracle
+    out = {}
+    # config 1
+    g = oracle.OracleGrid(2, (32, 32, 32), dt=0.05)
+    g.random_fields(SEED + 1, 0.1, 0.1)
+    g.gauss_project(1e-26)
+    h = opx.Handle(2, g.dims, dt=0.05, precision=N.OPX_F64, device=device)
+    h.upload(N.FIELD_U, g.U)
+    h.upload(N.FIELD_E, g.E)
+    h.initialize()
+    sim = oracle.OracleSimulation(g)
+    sim.initialize()
+    t = time.perf_counter()
+    for _ in range(100):
+        sim.step()
+    t_orc = time.perf_counter() - t
+    ms = h.time_steps(100)
+    U, E = h.download(N.FIELD_U), h.download(N.FIELD_E)
+    du = np.linalg.norm((U - g.U).reshape(-1, 4), axis=1).max()
+    ev = E.reshape(-1, 3)
+    eo = g.E.reshape(-1, 3)
+    de = (np.linalg.norm(ev - eo, axis=1) / np.maximum(np.linalg.norm(eo, axis=1), np.sqrt((eo ** 2).sum(1).mean()))).max()
+    bo, bd = g.bulk(), h.reduce()
+    out["config1_su2_fp64_32"] = {"steps": 100, "gpu_ms_per_step": ms / 100, "oracle_s_1thread": t_orc,
+                                  "max_rel_link_err": float(du), "max_rel_E_err": float(de),
+                                  "energy_rel_err": abs(bd.e2_total + bd.b2_total - bo[11] - bo[12]) / (bo[11] + bo[12]),
+                                  "gauss": bd.gauss, "bar": 1e-10}
+    h.close()
+    # config 3: FP32 against FP64 on the full lattice, and against the oracle on 32^3
+    res = {}
+    for dims, nsteps, key in (((128, 128, 128), 500, "gpu_fp64_128"), ((32, 32, 32), 500, "oracle_32")):
+        h64 = opx.Handle(3, dims, dt=0.05, precision=N.OPX_F64, device=device)
+        h64.init_random(SEED + 3, 0.2, 0.2)
+        h64.gauss_project(1e-26)
+        h32 = opx.Handle(3, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
+        U0, E0 = h64.download(N.FIELD_U), h64.download(N.FIELD_E)
+        h32.upload(N.FIELD_U, U0)
+        h32.upload(N.FIELD_E, E0)
+        h32.initialize()
+        if key == "oracle_32":
+            ref = oracle.OracleGrid(3, dims, dt=0.05)
+            ref.U[...] = U0
+            ref.E[...] = E0
+            ref.update_links()
+            nth = cpu_threads()
+            e_ref0 = ref.bulk()
+            for _ in range(nsteps):
+                ref.store_fields()
+                ref.update_grid_omp(nth)
+            h32.step(nsteps)
+            b = ref.bulk()
+            Ur, e_ref = ref.U, b[11] + b[12]
+        else:
+            h64.initialize()
+            h64.step(nsteps)
+            h32.step(nsteps)
+            o = h64.reduce()
+            Ur, e_ref = h64.download(N.FIELD_U), o.e2_total + o.b2_total
+        o32 = h32.reduce()
+        U32 = h32.download(N.FIELD_U)
+        d = np.linalg.norm((U32 - Ur).reshape(-1, 18), axis=1) / np.linalg.norm(Ur.reshape(-1, 18), axis=1)
+        res[key] = {"lattice": list(dims), "steps": nsteps, "energy_rel_err": abs(o32.e2_total + o32.b2_total - e_ref) / e_ref,
+                    "max_rel_link_err": float(d.max()), "mean_rel_link_err": float(d.mean())}
+        h64.close()
+        h32.close()
+    out["config3_fp32_errors"] = res
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -449,6 +570,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-cgc", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -587,6 +709,14 @@ def main():
     if not args.no_cgc and args.workload == "su3_fp32_128":
         cgc = bench_cgc(device)
 
+    configs = None
+    if rank == 0 and not args.no_configs and args.workload == "su3_fp32_128":
+        try:
+            configs = bench_configs(device)
+            configs["config5_differentiation"] = bench_differentiation(device)
+        except Exception as e:  # the headline stands without the extra legs
+            configs = {"skipped": str(e)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, U_host.array, E_host.array)
@@ -597,7 +727,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": w["prec"], "data": "synthetic",
                 "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64, "batched": batched,
-                "cgc_collision": cgc,
+                "cgc_collision": cgc, "configs": configs,
                 "reduce_ms": reduce_ms, "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
                 "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
         print(json.dumps(line), flush=True)
