@@ -644,6 +644,17 @@ def main():
     rms, rn = h.phase_times()
     h.set_profiling(False)
     reduce_ms = rms[N.PHASE_DIA] / max(rn[N.PHASE_DIA], 1)
+    # the reduction right after one step, as in a per-step diagnostics loop: B^2
+    # of U comes from the previous reduction's B^2 of Unext (one full reduction
+    # first, its mean time taken out)
+    h.set_profiling(True)
+    h.reduce()
+    for _ in range(10):
+        h.step(1)
+        h.reduce()
+    rms, rn = h.phase_times()
+    h.set_profiling(False)
+    reduce_after_step_ms = (rms[N.PHASE_DIA] - reduce_ms) / max(rn[N.PHASE_DIA] - 1, 1)
 
     # ---- the plain FP64 GPU path on the same lattice (same initial fields)
     fp64 = None
@@ -733,7 +744,8 @@ def main():
                 "config": config_for(w, args.workload), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "fp64_plain": fp64, "batched": batched,
                 "cgc_collision": cgc, "configs": configs,
-                "reduce_ms": reduce_ms, "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
+                "reduce_ms": reduce_ms, "reduce_after_step_ms": reduce_after_step_ms,
+                "energy_rel_change_over_run": abs(e1 - e0) / e0, "gauss_violation_end": o1.gauss,
                 "ic": {"cg_iterations": cg_it, "mean_g2_after_projection": g2}}
         print(json.dumps(line), flush=True)
     dist.close()

@@ -66,6 +66,18 @@ struct Ctx {
     unsigned *status_host = nullptr;
     long steps = 0;
     long launches = 0;
+    // Reuse of B^2 across reductions: a reduction right after one opx_step(ctx, 1)
+    // that followed a reduction takes B^2 of U from that reduction's B^2 of Unext
+    // (the same links after the swap).  api_calls counts the entry-point calls on
+    // the handle, so that any other call in between (an upload, an initial
+    // condition, a gauge transformation ...) disables the reuse.
+    long api_calls = 0;
+    long step1_call = -1;  // api_calls value of the last opx_step(ctx, 1)
+    struct {
+        long calls = -1, steps = -1;
+        const void *unext = nullptr;
+        double bn[3] = {0, 0, 0};  // B^2 of Unext, per direction, summed over the sites
+    } bcache;
     Particles P;
     // field solver: FastTYMSolver (imp_solver false) or ImplicitTYMSolver
     bool imp_solver = false;
@@ -87,7 +99,9 @@ int launch_implicit_update(Ctx &c);  // ImplicitTYMSolver.step in place of launc
 void launch_update_links(Ctx &c);
 void launch_reunit(Ctx &c, void *links);
 // ---- reductions (reduce_kernels.cu) ----
-void launch_bulk(Ctx &c);  // result in c.red_out[0..7]
+// result in c.red_out[0..10]: E^2[3], B^2 of U [3] (zero with skip_u), G^2, rho^2, B^2 of Unext [3]
+constexpr int BULK_COLUMNS = 11;
+void launch_bulk(Ctx &c, int skip_u);
 int reduction_blocks(long V);
 void launch_energy_density(Ctx &c, double *dev_out);
 void launch_projected_energy(Ctx &c, int dir, double *dev_out);

@@ -19,6 +19,35 @@ __host__ __device__ __forceinline__ void ksum_merge(KSum &a, const KSum &b) {
     a.c += b.c;
 }
 
+// NQ per-thread compensated running sums held in shared memory ([NQ][NT]
+// pairs, NT = blockDim.x): they live across a whole lattice loop, where the
+// registers are wanted for the site arithmetic.  A thread touches only its own
+// slots, so no synchronisation is needed until the block reduction.
+template <int NQ, int NT>
+struct SharedKSums {
+    double2 *a;
+    __device__ __forceinline__ void zero() const {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) a[q * NT + threadIdx.x] = make_double2(0.0, 0.0);
+    }
+    __device__ __forceinline__ void add(const double *p) const {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const double2 v = a[q * NT + threadIdx.x];
+            KSum k{v.x, v.y};
+            two_sum_add(k, p[q]);
+            a[q * NT + threadIdx.x] = make_double2(k.s, k.c);
+        }
+    }
+    __device__ __forceinline__ void load(KSum *acc) const {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const double2 v = a[q * NT + threadIdx.x];
+            acc[q] = KSum{v.x, v.y};
+        }
+    }
+};
+
 // Reduce NQ compensated sums over a block (blockDim.x a multiple of 32, at most
 // 1024).  Thread q < NQ of the block receives the block total of quantity q.
 template <int NQ>

@@ -26,35 +26,99 @@ template <> struct RedBounds<3, float> { static constexpr int minb = 4; };
 template <> struct RedBounds<3, double> { static constexpr int minb = 2; };
 constexpr int RED_THREADS = 128;
 
+// Columns of the partial sums: E^2[3], B^2 from U [3], G^2, rho^2, B^2 from
+// Unext [3].  B^2 of U and of Unext are kept apart so that a reduction right
+// after one step can take B^2 of U from the previous reduction's B^2 of Unext
+// (the same links; skip_u).
+constexpr int NQS = BULK_COLUMNS;
+
 template <int NC, typename R>
 __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
-                   const R *__restrict__ rho, const uint8_t *__restrict__ eval, Lat L, double *__restrict__ part) {
-    KSum acc[NQ];
-    bulk_accumulate<NC, R>(U, Unext, E, rho, eval, L, acc, (long)blockIdx.x * blockDim.x + threadIdx.x,
-                           (long)gridDim.x * blockDim.x);
-    // block reduction: warp shuffles then shared memory, fixed order
+                   const R *__restrict__ rho, const uint8_t *__restrict__ eval, Lat L, int skip_u,
+                   double *__restrict__ part) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
+    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V};
+    __shared__ double2 acc_sh[NQS * RED_THREADS];
+    const SharedKSums<NQS, RED_THREADS> sacc{acc_sh};
+    sacc.zero();
+    double p[NQS];
+#pragma unroll
+    for (int q = 0; q < NQS; q++) p[q] = 0.0;
+    int run = 0;
+    for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < L.V; s += (long)gridDim.x * blockDim.x) {
+        if (eval && !eval[s]) continue;
+        int x[3];
+        site_coords(L, s, x);
+        const Nbr nb = neighbours(L, s, x);
+#pragma unroll 1
+        for (int i = 0; i < 3; i++) {
+            R e[NA];
+            Ep.load_ro(i, s, e);
+            const double ev = sqr<R, NA>(e);
+            R b0[NA], b1[NA];
+            double bu = 0.0;
+            if (!skip_u) {
+                field_b<G, R>(Up, L, s, nb, i, b0);
+                bu = sqr<R, NA>(b0);
+            }
+            field_b<G, R>(Unp, L, s, nb, i, b1);
+            const double bn = sqr<R, NA>(b1);
+            if (i == 0) { p[0] += ev; p[3] += bu; p[8] += bn; }
+            else if (i == 1) { p[1] += ev; p[4] += bu; p[9] += bn; }
+            else { p[2] += ev; p[5] += bu; p[10] += bn; }
+        }
+        R gs[NA];
+        gauss_site<G, R>(Up, Ep, rho, L, s, nb, gs);
+        p[6] += sqr<R, NA>(gs);
+        if (rho) {
+            R r[NA];
+#pragma unroll
+            for (int a = 0; a < NA; a++) r[a] = __ldg(rho + (long)a * L.V + s);
+            p[7] += sqr<R, NA>(r);
+        }
+        if (++run == 32) {
+            sacc.add(p);
+#pragma unroll
+            for (int q = 0; q < NQS; q++) p[q] = 0.0;
+            run = 0;
+        }
+    }
+    sacc.add(p);
+    KSum acc[NQS];
+    sacc.load(acc);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const double uf = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
+        acc[i].s *= uf; acc[i].c *= uf;
+        acc[3 + i].s *= 0.5 * uf; acc[3 + i].c *= 0.5 * uf;
+        acc[8 + i].s *= 0.5 * uf; acc[8 + i].c *= 0.5 * uf;
+    }
     int q;
-    KSum v = block_reduce<NQ>(acc, q);
+    KSum v = block_reduce<NQS>(acc, q);
     if (q >= 0) {
-        part[((long)blockIdx.x * NQ + q) * 2] = v.s;
-        part[((long)blockIdx.x * NQ + q) * 2 + 1] = v.c;
+        part[((long)blockIdx.x * NQS + q) * 2] = v.s;
+        part[((long)blockIdx.x * NQS + q) * 2 + 1] = v.c;
     }
 }
 
 __global__ void k_bulk_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
-    // one warp per quantity: lanes take strided blocks, then a fixed-order shuffle tree
+    // one warp per column: lanes take strided blocks, then a fixed-order shuffle tree
     const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (q >= NQ) return;
+    if (q >= NQS) return;
     KSum v{0.0, 0.0};
     for (int b = lane; b < nblocks; b += 32)
-        ksum_merge(v, KSum{part[((long)b * NQ + q) * 2], part[((long)b * NQ + q) * 2 + 1]});
+        ksum_merge(v, KSum{part[((long)b * NQS + q) * 2], part[((long)b * NQS + q) * 2 + 1]});
     for (int o = 16; o > 0; o >>= 1) {
         KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
         ksum_merge(v, w);
     }
     if (lane == 0) out[q] = v.s + v.c;
 }
+
+int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
 
 // SU(3) FP32: two sites per thread in paired FP32 instructions (the
 // arithmetic of bulk_accumulate for sites sa and sb = sa + 32; the two lanes
@@ -63,16 +127,16 @@ template <typename I>
 __global__ void __launch_bounds__(RED_THREADS, 3)
     k_bulk_partial_su3f_pair(const float *__restrict__ U, const float *__restrict__ Unext,
                              const float *__restrict__ E, const float *__restrict__ rho,
-                             const uint8_t *__restrict__ eval, Lat L, double *__restrict__ part) {
+                             const uint8_t *__restrict__ eval, Lat L, int skip_u, double *__restrict__ part) {
     using namespace pr;
     const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
     const I npairs = (I)(((L.V + 63) >> 6) << 5);
-    KSum acc[NQ];
+    __shared__ double2 acc_sh[NQS * RED_THREADS];
+    const SharedKSums<NQS, RED_THREADS> sacc{acc_sh};
+    sacc.zero();
+    double p[NQS];
 #pragma unroll
-    for (int q = 0; q < NQ; q++) acc[q] = KSum{0.0, 0.0};
-    double p[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; q++) p[q] = 0.0;
+    for (int q = 0; q < NQS; q++) p[q] = 0.0;
     int run = 0;
     for (I t = (I)blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += (I)gridDim.x * blockDim.x) {
         const I sa = ((t >> 5) << 6) + (t & 31);
@@ -89,14 +153,6 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
         auto widen = [&](P v) { return (wa ? (double)v.x : 0.0) + (wb ? (double)v.y : 0.0); };
 #pragma unroll 1
         for (int d = 0; d < 3; d++) {
-            // E^2 of link d
-            const I eo = (I)d * 8 * V;
-            P e[8];
-#pragma unroll
-            for (int a = 0; a < 8; a++) e[a] = pp(__ldg(E + eo + (I)a * V + sa), __ldg(E + eo + (I)a * V + sb));
-            P se = mul2(e[0], e[0]);
-#pragma unroll
-            for (int a = 1; a < 8; a++) se = fma2(e[a], e[a], se);
             // B_d from U and Unext: U_j(x) U_k(x+j) U_j(x+k)^dagger U_k(x)^dagger, (d, j, k) cyclic
             const int j = d + 1 >= 3 ? d - 2 : d + 1, k = d + 2 >= 3 ? d - 1 : d + 2;
             const I pja = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], j), j, +1);
@@ -104,22 +160,24 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
             const I pka = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], k), k, +1);
             const I pkb = shift<I>(L, sb, pick(xb[0], xb[1], xb[2], k), k, +1);
             const P bf = bc(LatR<float>::bfac(L, d));
-            P sb2 = zero2();
+            P sbu = zero2(), sbn = zero2();
 #pragma unroll 1
-            for (int tt = 0; tt < 2; tt++) {
+            for (int tt = skip_u ? 1 : 0; tt < 2; tt++) {
                 const float *W = tt == 0 ? U : Unext;
                 const M Pq = mul_adj(mul_adj(mul(load<I>(W, nblk, j, sa, sb), load<I>(W, nblk, k, pja, pjb)),
                                              load<I>(W, nblk, j, pka, pkb)),
                                      load<I>(W, nblk, k, sa, sb));
                 P b[8];
                 proj(Pq, b);
+                P sb2 = zero2();
 #pragma unroll
                 for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); sb2 = fma2(b[a], b[a], sb2); }
+                if (tt == 0) sbu = sb2; else sbn = sb2;
             }
-            const double ev = widen(se), bv = widen(sb2);
-            if (d == 0) { p[0] += ev; p[3] += bv; }
-            else if (d == 1) { p[1] += ev; p[4] += bv; }
-            else { p[2] += ev; p[5] += bv; }
+            const double bu = widen(sbu), bn = widen(sbn);
+            if (d == 0) { p[3] += bu; p[8] += bn; }
+            else if (d == 1) { p[4] += bu; p[9] += bn; }
+            else { p[5] += bu; p[10] += bn; }
         }
         // Gauss: sum_i [E_i(x) - U_i(x-i)^dagger E_i(x-i) U_i(x-i)] gfac_i - rho(x)
         P gs[8];
@@ -136,6 +194,14 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
                 e0[a] = pp(__ldg(E + eo + (I)a * V + sa), __ldg(E + eo + (I)a * V + sb));
                 e1[a] = pp(__ldg(E + eo + (I)a * V + mia), __ldg(E + eo + (I)a * V + mib));
             }
+            // E^2 of link i at x
+            P se = mul2(e0[0], e0[0]);
+#pragma unroll
+            for (int a = 1; a < 8; a++) se = fma2(e0[a], e0[a], se);
+            const double ev = widen(se);
+            if (i == 0) p[0] += ev;
+            else if (i == 1) p[1] += ev;
+            else p[2] += ev;
             const M Ub = load<I>(U, nblk, i, mia, mib);
             herm_gen(mul(adj_mul(Ub, herm(e1)), Ub), tv);
             const P gf = bc(LatR<float>::gfac(L, i));
@@ -157,56 +223,74 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
         for (int a = 1; a < 8; a++) g2 = fma2(gs[a], gs[a], g2);
         p[6] += widen(g2);
         if (++run == 16) {
+            sacc.add(p);
 #pragma unroll
-            for (int q = 0; q < NQ; q++) { two_sum_add(acc[q], p[q]); p[q] = 0.0; }
+            for (int q = 0; q < NQS; q++) p[q] = 0.0;
             run = 0;
         }
     }
-#pragma unroll
-    for (int q = 0; q < NQ; q++) two_sum_add(acc[q], p[q]);
+    sacc.add(p);
+    KSum acc[NQS];
+    sacc.load(acc);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const double uf = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
         acc[i].s *= uf; acc[i].c *= uf;
         acc[3 + i].s *= 0.5 * uf; acc[3 + i].c *= 0.5 * uf;
+        acc[8 + i].s *= 0.5 * uf; acc[8 + i].c *= 0.5 * uf;
     }
     int q;
-    KSum v = block_reduce<NQ>(acc, q);
+    KSum v = block_reduce<NQS>(acc, q);
     if (q >= 0) {
-        part[((long)blockIdx.x * NQ + q) * 2] = v.s;
-        part[((long)blockIdx.x * NQ + q) * 2 + 1] = v.c;
+        part[((long)blockIdx.x * NQS + q) * 2] = v.s;
+        part[((long)blockIdx.x * NQS + q) * 2 + 1] = v.c;
     }
 }
 
-int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
+
+// Blocks of one kernel resident on the whole device at once: the grid-stride
+// reductions then run in a single wave with equal work per thread.
+template <typename K>
+static int resident_blocks(K kernel) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, RED_THREADS, 0);
+    return std::max(1, per_sm) * std::max(1, sms);
+}
 
 template <int NC, typename R>
-static void bulk_t(Ctx &c) {
+static void bulk_t(Ctx &c, int skip_u) {
+    int nb = c.red_blocks;
     if (NC == 3 && sizeof(R) == 4 && c.pair_kernel) {
-        if (link_elems(c.L.V, 18) < (1L << 31) - 64)
-            k_bulk_partial_su3f_pair<int><<<c.red_blocks, RED_THREADS, 0, c.stream>>>(
+        if (link_elems(c.L.V, 18) < (1L << 31) - 64) {
+            static const int wave = resident_blocks(k_bulk_partial_su3f_pair<int>);
+            nb = std::min(nb, wave);
+            k_bulk_partial_su3f_pair<int><<<nb, RED_THREADS, 0, c.stream>>>(
                 (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
-                c.red_part);
-        else
-            k_bulk_partial_su3f_pair<long><<<c.red_blocks, RED_THREADS, 0, c.stream>>>(
+                skip_u, c.red_part);
+        } else {
+            static const int wave = resident_blocks(k_bulk_partial_su3f_pair<long>);
+            nb = std::min(nb, wave);
+            k_bulk_partial_su3f_pair<long><<<nb, RED_THREADS, 0, c.stream>>>(
                 (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
-                c.red_part);
-        k_bulk_final<<<1, 32 * NQ, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
-        c.launches += 2;
-        return;
+                skip_u, c.red_part);
+        }
+    } else {
+        static const int wave = resident_blocks(k_bulk_partial<NC, R>);
+        nb = std::min(nb, wave);
+        k_bulk_partial<NC, R><<<nb, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
+                                                               (const R *)c.rho, c.eval, c.L, skip_u, c.red_part);
     }
-    k_bulk_partial<NC, R><<<c.red_blocks, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext,
-                                                                     (const R *)c.E, (const R *)c.rho, c.eval, c.L,
-                                                                     c.red_part);
-    k_bulk_final<<<1, 32 * NQ, 0, c.stream>>>(c.red_part, c.red_blocks, c.red_out);
+    k_bulk_final<<<1, 32 * NQS, 0, c.stream>>>(c.red_part, nb, c.red_out);
     c.launches += 2;
 }
 
-void launch_bulk(Ctx &c) {
+void launch_bulk(Ctx &c, int skip_u) {
     if (c.nc == 2) {
-        if (c.prec == OPX_F64) bulk_t<2, double>(c); else bulk_t<2, float>(c);
+        if (c.prec == OPX_F64) bulk_t<2, double>(c, skip_u); else bulk_t<2, float>(c, skip_u);
     } else {
-        if (c.prec == OPX_F64) bulk_t<3, double>(c); else bulk_t<3, float>(c);
+        if (c.prec == OPX_F64) bulk_t<3, double>(c, skip_u); else bulk_t<3, float>(c, skip_u);
     }
 }
 

@@ -1,0 +1,90 @@
+"""Reuse of B^2 between per-step reductions.
+
+opx_reduce right after opx_step(ctx, 1), which followed an opx_reduce, takes B^2
+of U from the previous reduction's B^2 of Unext (the same links after the
+storeFields swap) and sums only the plaquettes of Unext.  The observables must
+be bit-identical to a full recomputation: a twin handle on the same initial
+fields calls opx_synchronize between step and reduce, which disables the reuse.
+Any other entry point between the two reductions (an upload here) must disable
+it as well.  Every run is also checked against the CPU FP64 oracle once.
+"""
+import numpy as np
+import pytest
+
+import openpixi_gb300 as opx
+from openpixi_gb300 import _native as N
+from tests.helpers import oracle_ic, fresh
+
+pytestmark = pytest.mark.gpu
+
+
+def vec(o):
+    return np.array(list(o.e2) + list(o.b2) + [o.px, o.py, o.pz, o.gauss, o.rho2, o.e2_total, o.b2_total])
+
+
+def twin_handles(nc, dims, prec, reunit, seed, sigma, implicit=False):
+    g = fresh(oracle_ic(nc, dims, seed, sigma, sigma))
+    hs = []
+    for _ in range(2):
+        h = opx.Handle(nc, dims, a=g.a, dt=g.dt, g=g.g, precision=prec, reunit_every=reunit)
+        h.upload(N.FIELD_U, g.U)
+        h.upload(N.FIELD_E, g.E)
+        if implicit:
+            h.set_field_solver(N.SOLVER_IMPLICIT, 3, 0.0)
+        h.initialize()
+        hs.append(h)
+    return g, hs
+
+
+@pytest.mark.parametrize("nc,dims,prec,reunit,implicit", [
+    (2, (16, 12, 10), N.OPX_F64, 0, False),
+    (3, (12, 10, 14), N.OPX_F64, 0, False),
+    (3, (16, 16, 16), N.OPX_F32, 4, False),   # the paired SU(3) FP32 reduction, reunitarisation on
+    (2, (10, 8, 12), N.OPX_F32, 0, False),
+    (2, (8, 8, 8), N.OPX_F64, 0, True),       # ImplicitTYMSolver steps
+])
+def test_reuse_bit_identical(native, orc, nc, dims, prec, reunit, implicit):
+    g, (a, b) = twin_handles(nc, dims, prec, reunit, 77, 0.25, implicit)
+    ra, rb = [a.reduce()], [b.reduce()]
+    for k in range(12):
+        a.step(1)
+        ra.append(a.reduce())
+        b.step(1)
+        b.synchronize()  # any entry point in between: recompute everything
+        rb.append(b.reduce())
+    for oa, ob in zip(ra, rb):
+        assert np.array_equal(vec(oa), vec(ob)), (vec(oa), vec(ob))
+    if prec == N.OPX_F64 and not implicit:
+        sim = orc.OracleSimulation(g)
+        sim.initialize()
+        for _ in range(12):
+            sim.step()
+        ref = g.bulk()
+        got = vec(ra[-1])
+        et = ref[11] + ref[12]
+        assert abs(got[11] + got[12] - et) <= 1e-12 * abs(et)
+        assert np.all(np.abs(got[:9] - ref[:9]) <= 1e-12 * abs(et))
+
+
+def test_reuse_disabled_by_other_calls(native):
+    """step(1), then an upload of other links, then reduce: B^2 of U must come
+    from the uploaded links, not from the previous reduction."""
+    rng = np.random.default_rng(5)
+    _, (a, b) = twin_handles(2, (12, 12, 12), N.OPX_F64, 0, 91, 0.3)
+    a.reduce()
+    b.reduce()
+    a.step(1)
+    b.step(1)
+    U = a.download(N.FIELD_U)
+    q = U + rng.normal(0, 0.05, U.shape)
+    q /= np.linalg.norm(q, axis=-1, keepdims=True)
+    a.upload(N.FIELD_U, q)
+    b.upload(N.FIELD_U, q)
+    b.synchronize()
+    oa, ob = a.reduce(), b.reduce()
+    assert np.array_equal(vec(oa), vec(ob))
+    # and the reuse after a multi-step call stays off as well
+    a.step(3)
+    b.step(3)
+    b.synchronize()
+    assert np.array_equal(vec(a.reduce()), vec(b.reduce()))
