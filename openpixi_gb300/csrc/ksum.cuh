@@ -30,14 +30,15 @@ struct SharedKSums {
 #pragma unroll
         for (int q = 0; q < NQ; q++) a[q * NT + threadIdx.x] = make_double2(0.0, 0.0);
     }
+    __device__ __forceinline__ void add1(int q, double x) const {
+        const double2 v = a[q * NT + threadIdx.x];
+        KSum k{v.x, v.y};
+        two_sum_add(k, x);
+        a[q * NT + threadIdx.x] = make_double2(k.s, k.c);
+    }
     __device__ __forceinline__ void add(const double *p) const {
 #pragma unroll
-        for (int q = 0; q < NQ; q++) {
-            const double2 v = a[q * NT + threadIdx.x];
-            KSum k{v.x, v.y};
-            two_sum_add(k, p[q]);
-            a[q * NT + threadIdx.x] = make_double2(k.s, k.c);
-        }
+        for (int q = 0; q < NQ; q++) add1(q, p[q]);
     }
     __device__ __forceinline__ void load(KSum *acc) const {
 #pragma unroll

@@ -121,8 +121,12 @@ __global__ void k_bulk_final(const double *__restrict__ part, int nblocks, doubl
 int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
 
 // SU(3) FP32: two sites per thread in paired FP32 instructions (the
-// arithmetic of bulk_accumulate for sites sa and sb = sa + 32; the two lanes
-// are summed into the thread's partial sums).
+// arithmetic of bulk_accumulate for sites sa and sb = sa + 32).  The per-site
+// values are FP32; a thread sums the two lanes and runs of 32 pair-iterations
+// (64 sites) in FP32 with Kahan compensation (every value is a sum of squares,
+// so the running sum dominates each term), then widens each run into the FP64
+// compensated sums.  The FP64 pipe is narrow on this part: one FP64 add per
+// column per site kept it half busy.
 template <typename I>
 __global__ void __launch_bounds__(RED_THREADS, 3)
     k_bulk_partial_su3f_pair(const float *__restrict__ U, const float *__restrict__ Unext,
@@ -134,9 +138,23 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
     __shared__ double2 acc_sh[NQS * RED_THREADS];
     const SharedKSums<NQS, RED_THREADS> sacc{acc_sh};
     sacc.zero();
-    double p[NQS];
+    float rs[NQS], rc[NQS];  // FP32 Kahan run sums and their compensations
 #pragma unroll
-    for (int q = 0; q < NQS; q++) p[q] = 0.0;
+    for (int q = 0; q < NQS; q++) { rs[q] = 0.f; rc[q] = 0.f; }
+    auto kadd = [&](int q, float x) {
+        const float y = x - rc[q];
+        const float t = rs[q] + y;
+        rc[q] = (t - rs[q]) - y;
+        rs[q] = t;
+    };
+    auto flush = [&]() {
+#pragma unroll
+        for (int q = 0; q < NQS; q++) {
+            sacc.add1(q, (double)rs[q] - (double)rc[q]);
+            rs[q] = 0.f;
+            rc[q] = 0.f;
+        }
+    };
     int run = 0;
     for (I t = (I)blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += (I)gridDim.x * blockDim.x) {
         const I sa = ((t >> 5) << 6) + (t & 31);
@@ -150,7 +168,7 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
         int xa[3], xb[3];
         coords<I>(L, sa, xa);
         coords<I>(L, sb, xb);
-        auto widen = [&](P v) { return (wa ? (double)v.x : 0.0) + (wb ? (double)v.y : 0.0); };
+        auto lanes = [&](P v) { return (wa ? v.x : 0.f) + (wb ? v.y : 0.f); };
 #pragma unroll 1
         for (int d = 0; d < 3; d++) {
             // B_d from U and Unext: U_j(x) U_k(x+j) U_j(x+k)^dagger U_k(x)^dagger, (d, j, k) cyclic
@@ -174,10 +192,11 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
                 for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); sb2 = fma2(b[a], b[a], sb2); }
                 if (tt == 0) sbu = sb2; else sbn = sb2;
             }
-            const double bu = widen(sbu), bn = widen(sbn);
-            if (d == 0) { p[3] += bu; p[8] += bn; }
-            else if (d == 1) { p[4] += bu; p[9] += bn; }
-            else { p[5] += bu; p[10] += bn; }
+            // constant indices keep the run sums in registers
+            const float bu = lanes(sbu), bn = lanes(sbn);
+            if (d == 0) { if (!skip_u) kadd(3, bu); kadd(8, bn); }
+            else if (d == 1) { if (!skip_u) kadd(4, bu); kadd(9, bn); }
+            else { if (!skip_u) kadd(5, bu); kadd(10, bn); }
         }
         // Gauss: sum_i [E_i(x) - U_i(x-i)^dagger E_i(x-i) U_i(x-i)] gfac_i - rho(x)
         P gs[8];
@@ -198,10 +217,10 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
             P se = mul2(e0[0], e0[0]);
 #pragma unroll
             for (int a = 1; a < 8; a++) se = fma2(e0[a], e0[a], se);
-            const double ev = widen(se);
-            if (i == 0) p[0] += ev;
-            else if (i == 1) p[1] += ev;
-            else p[2] += ev;
+            const float ev = lanes(se);
+            if (i == 0) kadd(0, ev);
+            else if (i == 1) kadd(1, ev);
+            else kadd(2, ev);
             const M Ub = load<I>(U, nblk, i, mia, mib);
             herm_gen(mul(adj_mul(Ub, herm(e1)), Ub), tv);
             const P gf = bc(LatR<float>::gfac(L, i));
@@ -216,20 +235,18 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
                 gs[a] = sub2(gs[a], r);
                 r2 = fma2(r, r, r2);
             }
-            p[7] += widen(r2);
+            kadd(7, lanes(r2));
         }
         P g2 = mul2(gs[0], gs[0]);
 #pragma unroll
         for (int a = 1; a < 8; a++) g2 = fma2(gs[a], gs[a], g2);
-        p[6] += widen(g2);
-        if (++run == 16) {
-            sacc.add(p);
-#pragma unroll
-            for (int q = 0; q < NQS; q++) p[q] = 0.0;
+        kadd(6, lanes(g2));
+        if (++run == 32) {
+            flush();
             run = 0;
         }
     }
-    sacc.add(p);
+    flush();
     KSum acc[NQS];
     sacc.load(acc);
 #pragma unroll
