@@ -49,27 +49,47 @@ struct SharedKSums {
     }
 };
 
-// Reduce NQ compensated sums over a block (blockDim.x a multiple of 32, at most
+// Plain FP64 per-thread sums in shared memory ([NQ][NT]), for values that
+// carry FP32 rounding already (the FP32 run sums of the paired SU(3) kernels):
+// one FP64 add per column per flush.
+template <int NQ, int NT>
+struct SharedSums {
+    double *a;
+    __device__ __forceinline__ void zero() const {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) a[q * NT + threadIdx.x] = 0.0;
+    }
+    __device__ __forceinline__ void add1(int q, double x) const { a[q * NT + threadIdx.x] += x; }
+    __device__ __forceinline__ void load(KSum *acc) const {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) acc[q] = KSum{a[q * NT + threadIdx.x], 0.0};
+    }
+};
+
+// Reduce NQ per-thread sums over a block (blockDim.x a multiple of 32, at most
 // 1024).  Thread q < NQ of the block receives the block total of quantity q.
+// Each thread's compensated sum collapses to one double, the lanes of a warp
+// are added in a fixed shuffle tree (five roundings deep) and the warps in
+// order with compensation.  The tree keeps the FP64 instruction count low: the
+// FP64 pipe of this part is narrow, and a compensated shuffle tree over eleven
+// columns took a fifth of a whole-lattice reduction.
 template <int NQ>
 __device__ __forceinline__ KSum block_reduce(KSum *acc, int &qout) {
-    __shared__ double sh_s[NQ][32], sh_c[NQ][32];
+    __shared__ double sh[NQ][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
-        KSum v = acc[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
-            ksum_merge(v, w);
-        }
-        if (lane == 0) { sh_s[q][warp] = v.s; sh_c[q][warp] = v.c; }
+        double v = acc[q].s + acc[q].c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[q][warp] = v;
     }
     __syncthreads();
     KSum v{0.0, 0.0};
     qout = -1;
     if (threadIdx.x < NQ) {
         const int q = threadIdx.x;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) ksum_merge(v, KSum{sh_s[q][w], sh_c[q][w]});
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) two_sum_add(v, sh[q][w]);
         qout = q;
     }
     return v;

@@ -4,8 +4,10 @@
 //       (physics/measurements/FieldMeasurements.java:68-231) as used by
 //       BulkQuantitiesInTime.calculate (diagnostics/methods/BulkQuantitiesInTime.java:83-121).
 //       One pass computes all of them (the reference makes six lattice passes).
-//       Per-site values are formed in the storage precision and accumulated in
-//       FP64 with compensated (Neumaier/TwoSum) sums; the block partials are
+//       Per-site values are formed in the storage precision; each thread
+//       accumulates them in FP64 with compensated (Neumaier/TwoSum) sums (FP64
+//       storage) or in FP32 Kahan runs added to an FP64 sum (FP32 storage); a
+//       block adds its threads in a fixed FP64 tree and the block partials are
 //       combined by one block in a fixed order, so results are deterministic.
 //   k_energy_density   : EnergyDensity.ComponentComputation (EnergyDensity.java:119-166)
 //   k_projected_energy : ProjectedEnergyDensity.EnergyDensityComputation (:114-179)
@@ -124,9 +126,9 @@ int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREAD
 // arithmetic of bulk_accumulate for sites sa and sb = sa + 32).  The per-site
 // values are FP32; a thread sums the two lanes and runs of 32 pair-iterations
 // (64 sites) in FP32 with Kahan compensation (every value is a sum of squares,
-// so the running sum dominates each term), then widens each run into the FP64
-// compensated sums.  The FP64 pipe is narrow on this part: one FP64 add per
-// column per site kept it half busy.
+// so the running sum dominates each term), then adds each run to a plain FP64
+// sum.  The FP64 pipe is narrow on this part: one FP64 add per column per site
+// kept it half busy.
 template <typename I>
 __global__ void __launch_bounds__(RED_THREADS, 3)
     k_bulk_partial_su3f_pair(const float *__restrict__ U, const float *__restrict__ Unext,
@@ -135,8 +137,8 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
     using namespace pr;
     const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
     const I npairs = (I)(((L.V + 63) >> 6) << 5);
-    __shared__ double2 acc_sh[NQS * RED_THREADS];
-    const SharedKSums<NQS, RED_THREADS> sacc{acc_sh};
+    __shared__ double acc_sh[NQS * RED_THREADS];
+    const SharedSums<NQS, RED_THREADS> sacc{acc_sh};
     sacc.zero();
     float rs[NQS], rc[NQS];  // FP32 Kahan run sums and their compensations
 #pragma unroll
