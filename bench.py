@@ -699,14 +699,19 @@ def main():
         h2.upload(N.FIELD_U, U_host.array)
         h2.upload(N.FIELD_E, E_host.array)
         h2.initialize()
+        t_in = time.perf_counter()
         for k in range(args.steps):
             h2.step(1)
             h2.reduce()
+        t_loop = time.perf_counter()
         h2.download(N.FIELD_U, out=U_host.array)
         h2.download(N.FIELD_E, out=E_host.array)
-        el = time.perf_counter() - t
+        t_out = time.perf_counter()
+        el = t_out - t
         el = dist.max(el)
         e2e = {"value": world * links * args.steps / el, "unit": METRIC,
+               "upload_ms": (t_in - t) * 1e3, "loop_ms_per_step": (t_loop - t_in) * 1e3 / args.steps,
+               "download_ms": (t_out - t_loop) * 1e3,
                "h2d_bytes_per_step": he / args.steps,
                "d2h_bytes_per_step": obs_bytes + he / args.steps,
                "note": "Simulation.step through the C ABI with the BulkQuantities observables (13 FP64 "

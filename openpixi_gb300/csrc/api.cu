@@ -27,10 +27,17 @@ Ctx &opx::ctx_of(opx_ctx *h) {
     return h->c;
 }
 
+// API_CHECK for entry points that may change the fields or the masks (counted,
+// so that the B^2 reuse of opx_reduce sees them); API_CHECK_RO for the ones
+// that only read.
 #define API_CHECK(ctx)                                   \
     do {                                                 \
         if (!(ctx)) return OPX_ERR_INVALID;              \
         (ctx)->c.api_calls++;                            \
+    } while (0)
+#define API_CHECK_RO(ctx)                                \
+    do {                                                 \
+        if (!(ctx)) return OPX_ERR_INVALID;              \
     } while (0)
 
 static int cuda_fail(Ctx &c, const char *where, cudaError_t e) {
@@ -220,7 +227,7 @@ int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int la
 }
 
 int opx_download(opx_ctx *ctx, int field, double *host, size_t count, int layout) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     size_t n;
     int ndir;
@@ -404,21 +411,20 @@ int opx_set_field_solver(opx_ctx *ctx, int kind, int iterations, double damping)
 }
 
 int opx_synchronize(opx_ctx *ctx) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     return sync_check(ctx->c, "opx_synchronize");
 }
 
 long opx_steps_done(const opx_ctx *ctx) { return ctx ? ctx->c.steps : -1; }
 
 int opx_reduce(opx_ctx *ctx, opx_observables *out) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (!out) { c.err = "opx_reduce: null output"; return OPX_ERR_INVALID; }
-    // this call follows opx_step(ctx, 1), which followed the last reduction:
-    // U now is the Unext that reduction summed B^2 over
-    const bool reuse = c.bcache.calls >= 0 && c.api_calls == c.bcache.calls + 2 &&
-                       c.step1_call == c.bcache.calls + 1 && c.steps == c.bcache.steps + 1 &&
-                       c.U == c.bcache.unext;
+    // the only call since the last reduction that could change the fields was
+    // opx_step(ctx, 1): U now is the Unext that reduction summed B^2 over
+    const bool reuse = c.bcache.calls >= 0 && c.api_calls == c.bcache.calls + 1 && c.step1_call == c.api_calls &&
+                       c.steps == c.bcache.steps + 1 && c.U == c.bcache.unext;
     c.bcache.calls = -1;
     phase_begin(c);
     launch_bulk(c, reuse ? 1 : 0);
@@ -457,7 +463,7 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out) {
 }
 
 int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (!host_out || count != (size_t)c.L.V) { c.err = "opx_energy_density: output must hold V doubles"; return OPX_ERR_INVALID; }
     int rc = ensure_staging(c, c.L.V);
@@ -468,7 +474,7 @@ int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count) {
 }
 
 int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (dir < 0 || dir > 2) { c.err = "opx_projected_energy: dir must be 0, 1 or 2"; return OPX_ERR_INVALID; }
     const size_t n = 4 * (size_t)c.L.n[dir];
@@ -481,7 +487,7 @@ int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) 
 }
 
 int opx_projected_poynting(opx_ctx *ctx, int dir, double *host_out, size_t count) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (dir < 0 || dir > 2) { c.err = "opx_projected_poynting: dir must be 0, 1 or 2"; return OPX_ERR_INVALID; }
     if (c.nc != 2) {
@@ -499,7 +505,7 @@ int opx_projected_poynting(opx_ctx *ctx, int dir, double *host_out, size_t count
 }
 
 int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     const size_t n = (size_t)c.L.V * c.na;
     if (!host_out || count != n) { c.err = "opx_gauss_field: output must hold V*ngen doubles"; return OPX_ERR_INVALID; }
@@ -553,7 +559,7 @@ int opx_particles_upload(opx_ctx *ctx, const opx_particles *p) {
 }
 
 int opx_particles_download(opx_ctx *ctx, opx_particles *p) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (!p || p->n != c.P.n) { c.err = "opx_particles_download: n must equal the uploaded count"; return OPX_ERR_INVALID; }
     const long n = p->n;
@@ -593,7 +599,7 @@ long opx_particles_count(const opx_ctx *ctx) { return ctx ? ctx->c.P.n : -1; }
 int opx_super_groups(const opx_ctx *ctx) { return ctx ? (int)ctx->c.sg.size() : -1; }
 
 int opx_super_download(opx_ctx *ctx, int group, int *orientation, long *n, long *base, double *Q, size_t count) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (group < 0 || group >= (int)c.sg.size()) { c.err = "opx_super_download: no such group"; return OPX_ERR_INVALID; }
     const SuperGroup &G = c.sg[group];
@@ -668,7 +674,7 @@ int opx_gauss_project(opx_ctx *ctx, double tol_g2, int maxit, int *iters, double
 }
 
 int opx_set_profiling(opx_ctx *ctx, int on) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     c.profiling = on != 0;
     for (int k = 0; k < OPX_NUM_PHASES; k++) { c.phase_ms[k] = 0; c.phase_n[k] = 0; }
@@ -676,7 +682,7 @@ int opx_set_profiling(opx_ctx *ctx, int on) {
 }
 
 int opx_phase_times(opx_ctx *ctx, double *ms, long *counts, int nphases) {
-    API_CHECK(ctx);
+    API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     for (int k = 0; k < nphases && k < OPX_NUM_PHASES; k++) {
         if (ms) ms[k] = c.phase_ms[k];

@@ -66,11 +66,13 @@ struct Ctx {
     unsigned *status_host = nullptr;
     long steps = 0;
     long launches = 0;
-    // Reuse of B^2 across reductions: a reduction right after one opx_step(ctx, 1)
+    // Reuse of B^2 across reductions: a reduction after one opx_step(ctx, 1)
     // that followed a reduction takes B^2 of U from that reduction's B^2 of Unext
-    // (the same links after the swap).  api_calls counts the entry-point calls on
-    // the handle, so that any other call in between (an upload, an initial
-    // condition, a gauge transformation ...) disables the reuse.
+    // (the same links after the swap).  api_calls counts the entry-point calls
+    // that may change the fields or the masks (all but the read-only ones:
+    // downloads, reductions, diagnostics, profiling), so that any other such call
+    // in between (an upload, an initial condition, a gauge transformation ...)
+    // disables the reuse.
     long api_calls = 0;
     long step1_call = -1;  // api_calls value of the last opx_step(ctx, 1)
     struct {
