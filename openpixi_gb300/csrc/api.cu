@@ -78,7 +78,7 @@ static void fill_identity(Ctx &c, void *U) {
 static void release(Ctx &c) {
     cpic_free(c);
     super_free(c);
-    void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.status,
+    void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.red_count, c.status,
                    c.imp_Ua, c.imp_Ub, c.imp_E};
     for (void *p : dev) if (p) cudaFree(p);
     if (c.red_host) cudaFreeHost(c.red_host);
@@ -139,6 +139,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     al((void **)&c.red_part,
        sizeof(double) * 2 * BULK_COLUMNS * std::max(c.red_blocks, 2 * c.L.n[0] + 2 * c.L.n[1] + 2 * c.L.n[2]));
     al((void **)&c.red_out, sizeof(double) * 16);
+    al((void **)&c.red_count, sizeof(unsigned));
     al((void **)&c.status, sizeof(unsigned));
     if (ok && cudaMallocHost((void **)&c.red_host, sizeof(double) * 16) != cudaSuccess) ok = false;
     if (ok && cudaMallocHost((void **)&c.status_host, sizeof(unsigned)) != cudaSuccess) ok = false;
@@ -156,6 +157,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     cudaMemsetAsync(c.J, 0, nE * c.rsize, c.stream);
     cudaMemsetAsync(c.rho, 0, (size_t)V * c.na * c.rsize, c.stream);
     cudaMemsetAsync(c.status, 0, sizeof(unsigned), c.stream);
+    if (c.red_count) cudaMemsetAsync(c.red_count, 0, sizeof(unsigned), c.stream);
     if (sync_check(c, "opx_create") != OPX_OK) {
         g_create_error = c.err;
         release(c);
@@ -199,6 +201,23 @@ static int field_count(const Ctx &c, int field, int layout, size_t *n, int *ndir
     return OPX_ERR_INVALID;
 }
 
+// The device address of a page-locked host buffer of n doubles (cudaMallocHost
+// or cudaHostRegister memory, both ends mapped at one offset), or null for
+// pageable memory.  The conversion kernels read and write page-locked buffers
+// directly over the host link; pageable ones go through the staging copy.
+static double *device_view(const void *host, size_t n) {
+    cudaPointerAttributes a0, a1;
+    const char *first = (const char *)host, *last = first + n * sizeof(double) - 1;
+    if (cudaPointerGetAttributes(&a0, first) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if ((const char *)a1.devicePointer - (const char *)a0.devicePointer != last - first) return nullptr;
+    return (double *)a0.devicePointer;
+}
+
 int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int layout) {
     API_CHECK(ctx);
     Ctx &c = ctx->c;
@@ -212,16 +231,20 @@ int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int la
         c.err = "opx_upload: count " + std::to_string(count) + " != expected " + std::to_string(n);
         return OPX_ERR_INVALID;
     }
-    int rc = ensure_staging(c, n);
-    if (rc) return rc;
-    cudaError_t e = cudaMemcpyAsync(c.staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c.stream);
-    if (e != cudaSuccess) return cuda_fail(c, "opx_upload", e);
+    const double *src = device_view(host, n);
+    if (!src) {
+        int rc = ensure_staging(c, n);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(c.staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        if (e != cudaSuccess) return cuda_fail(c, "opx_upload", e);
+        src = c.staging;
+    }
     switch (field) {
-    case OPX_FIELD_U: launch_links_from_ref(c, c.staging, c.U); break;
-    case OPX_FIELD_UNEXT: launch_links_from_ref(c, c.staging, c.Unext); break;
-    case OPX_FIELD_E: launch_alg_from_host(c, c.staging, c.E, 3, layout); break;
-    case OPX_FIELD_J: launch_alg_from_host(c, c.staging, c.J, 3, layout); c.j_nonzero = true; break;
-    case OPX_FIELD_RHO: launch_alg_from_host(c, c.staging, c.rho, 1, layout); break;
+    case OPX_FIELD_U: launch_links_from_ref(c, src, c.U); break;
+    case OPX_FIELD_UNEXT: launch_links_from_ref(c, src, c.Unext); break;
+    case OPX_FIELD_E: launch_alg_from_host(c, src, c.E, 3, layout); break;
+    case OPX_FIELD_J: launch_alg_from_host(c, src, c.J, 3, layout); c.j_nonzero = true; break;
+    case OPX_FIELD_RHO: launch_alg_from_host(c, src, c.rho, 1, layout); break;
     }
     return sync_check(c, "opx_upload");
 }
@@ -239,17 +262,24 @@ int opx_download(opx_ctx *ctx, int field, double *host, size_t count, int layout
         c.err = "opx_download: count " + std::to_string(count) + " != expected " + std::to_string(n);
         return OPX_ERR_INVALID;
     }
-    int rc = ensure_staging(c, n);
-    if (rc) return rc;
-    switch (field) {
-    case OPX_FIELD_U: launch_links_to_ref(c, c.U, c.staging); break;
-    case OPX_FIELD_UNEXT: launch_links_to_ref(c, c.Unext, c.staging); break;
-    case OPX_FIELD_E: launch_alg_to_host(c, c.E, c.staging, 3, layout); break;
-    case OPX_FIELD_J: launch_alg_to_host(c, c.J, c.staging, 3, layout); break;
-    case OPX_FIELD_RHO: launch_alg_to_host(c, c.rho, c.staging, 1, layout); break;
+    double *dst = device_view(host, n);
+    const bool direct = dst != nullptr;
+    if (!direct) {
+        int rc = ensure_staging(c, n);
+        if (rc) return rc;
+        dst = c.staging;
     }
-    cudaError_t e = cudaMemcpyAsync(host, c.staging, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
-    if (e != cudaSuccess) return cuda_fail(c, "opx_download", e);
+    switch (field) {
+    case OPX_FIELD_U: launch_links_to_ref(c, c.U, dst); break;
+    case OPX_FIELD_UNEXT: launch_links_to_ref(c, c.Unext, dst); break;
+    case OPX_FIELD_E: launch_alg_to_host(c, c.E, dst, 3, layout); break;
+    case OPX_FIELD_J: launch_alg_to_host(c, c.J, dst, 3, layout); break;
+    case OPX_FIELD_RHO: launch_alg_to_host(c, c.rho, dst, 1, layout); break;
+    }
+    if (!direct) {
+        cudaError_t e = cudaMemcpyAsync(host, c.staging, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        if (e != cudaSuccess) return cuda_fail(c, "opx_download", e);
+    }
     return sync_check(c, "opx_download");
 }
 

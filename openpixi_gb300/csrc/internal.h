@@ -61,6 +61,7 @@ struct Ctx {
     double *red_part = nullptr;
     int red_blocks = 0;
     double *red_out = nullptr;     // device
+    unsigned *red_count = nullptr; // device: blocks of the running reduction that have finished
     double *red_host = nullptr;    // pinned
     unsigned *status = nullptr;    // device status word
     unsigned *status_host = nullptr;

@@ -1,6 +1,6 @@
 // reduce_kernels.cu -- whole-lattice reductions and per-cell diagnostics.
 //
-//   k_bulk_partial / k_bulk_final : FieldMeasurements E^2, B^2, Gauss, rho^2
+//   k_bulk_partial(_su3f_pair) : FieldMeasurements E^2, B^2, Gauss, rho^2
 //       (physics/measurements/FieldMeasurements.java:68-231) as used by
 //       BulkQuantitiesInTime.calculate (diagnostics/methods/BulkQuantitiesInTime.java:83-121).
 //       One pass computes all of them (the reference makes six lattice passes).
@@ -34,11 +34,41 @@ constexpr int RED_THREADS = 128;
 // (the same links; skip_u).
 constexpr int NQS = BULK_COLUMNS;
 
+// The last block of a reduction to finish combines the block partials: warp w
+// takes columns w, w + nwarps, ...; its lanes stride over the blocks with
+// compensated sums and a fixed shuffle tree adds the lanes.  So a reduction is
+// one launch.  Each block publishes its partials, fences and draws a ticket;
+// the block that draws the last ticket reads every partial (through L2) and
+// resets the counter for the next launch on the stream.  No block waits on
+// another.
+template <int NQ>
+__device__ __forceinline__ void last_block_combine(const double *part, unsigned *count, double *out) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    for (int q = warp; q < NQ; q += nw) {
+        KSum v{0.0, 0.0};
+        for (int b = lane; b < (int)gridDim.x; b += 32)
+            ksum_merge(v, KSum{__ldcg(part + ((long)b * NQ + q) * 2), __ldcg(part + ((long)b * NQ + q) * 2 + 1)});
+        for (int o = 16; o > 0; o >>= 1) {
+            KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
+            ksum_merge(v, w);
+        }
+        if (lane == 0) out[q] = v.s + v.c;
+    }
+    if (threadIdx.x == 0) *count = 0u;
+}
+
 template <int NC, typename R>
 __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
                    const R *__restrict__ rho, const uint8_t *__restrict__ eval, Lat L, int skip_u,
-                   double *__restrict__ part) {
+                   double *__restrict__ part, unsigned *__restrict__ count, double *__restrict__ out) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
@@ -104,20 +134,7 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
         part[((long)blockIdx.x * NQS + q) * 2] = v.s;
         part[((long)blockIdx.x * NQS + q) * 2 + 1] = v.c;
     }
-}
-
-__global__ void k_bulk_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
-    // one warp per column: lanes take strided blocks, then a fixed-order shuffle tree
-    const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (q >= NQS) return;
-    KSum v{0.0, 0.0};
-    for (int b = lane; b < nblocks; b += 32)
-        ksum_merge(v, KSum{part[((long)b * NQS + q) * 2], part[((long)b * NQS + q) * 2 + 1]});
-    for (int o = 16; o > 0; o >>= 1) {
-        KSum w{__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o)};
-        ksum_merge(v, w);
-    }
-    if (lane == 0) out[q] = v.s + v.c;
+    last_block_combine<NQS>(part, count, out);
 }
 
 int reduction_blocks(long V) { return (int)std::min<long>(grid_for(V, RED_THREADS), 8L * 152); }
@@ -133,7 +150,8 @@ template <typename I>
 __global__ void __launch_bounds__(RED_THREADS, 3)
     k_bulk_partial_su3f_pair(const float *__restrict__ U, const float *__restrict__ Unext,
                              const float *__restrict__ E, const float *__restrict__ rho,
-                             const uint8_t *__restrict__ eval, Lat L, int skip_u, double *__restrict__ part) {
+                             const uint8_t *__restrict__ eval, Lat L, int skip_u, double *__restrict__ part,
+                             unsigned *__restrict__ count, double *__restrict__ out) {
     using namespace pr;
     const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
     const I npairs = (I)(((L.V + 63) >> 6) << 5);
@@ -264,6 +282,7 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
         part[((long)blockIdx.x * NQS + q) * 2] = v.s;
         part[((long)blockIdx.x * NQS + q) * 2 + 1] = v.c;
     }
+    last_block_combine<NQS>(part, count, out);
 }
 
 
@@ -287,22 +306,22 @@ static void bulk_t(Ctx &c, int skip_u) {
             nb = std::min(nb, wave);
             k_bulk_partial_su3f_pair<int><<<nb, RED_THREADS, 0, c.stream>>>(
                 (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
-                skip_u, c.red_part);
+                skip_u, c.red_part, c.red_count, c.red_out);
         } else {
             static const int wave = resident_blocks(k_bulk_partial_su3f_pair<long>);
             nb = std::min(nb, wave);
             k_bulk_partial_su3f_pair<long><<<nb, RED_THREADS, 0, c.stream>>>(
                 (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
-                skip_u, c.red_part);
+                skip_u, c.red_part, c.red_count, c.red_out);
         }
     } else {
         static const int wave = resident_blocks(k_bulk_partial<NC, R>);
         nb = std::min(nb, wave);
         k_bulk_partial<NC, R><<<nb, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
-                                                               (const R *)c.rho, c.eval, c.L, skip_u, c.red_part);
+                                                               (const R *)c.rho, c.eval, c.L, skip_u, c.red_part,
+                                                               c.red_count, c.red_out);
     }
-    k_bulk_final<<<1, 32 * NQS, 0, c.stream>>>(c.red_part, nb, c.red_out);
-    c.launches += 2;
+    c.launches += 1;
 }
 
 void launch_bulk(Ctx &c, int skip_u) {
