@@ -116,7 +116,13 @@ void opx_destroy(opx_ctx *ctx);
 const char *opx_last_error(const opx_ctx *ctx);
 int opx_version(void);
 
-/* ---- host <-> device (the Grid getters/setters, Grid.java:126-261) ---- */
+/* ---- host <-> device (the Grid getters/setters, Grid.java:126-261) ----
+ * host holds count doubles in the reference's per-cell layout (OPX_LAYOUT_REF)
+ * or generator components (OPX_LAYOUT_GEN).  A page-locked buffer
+ * (opx_host_alloc, cudaMallocHost, cudaHostRegister) is read or written by the
+ * conversion kernels directly; a pageable one goes through a device staging
+ * copy (allocated on first use, kept by the handle).  Both return after the
+ * transfer is complete. */
 int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int layout);
 int opx_download(opx_ctx *ctx, int field, double *host, size_t count, int layout);
 /* Cell.isActive / Cell.isEvaluatable masks; NULL resets to all-true
