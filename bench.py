@@ -44,7 +44,7 @@ WORKLOADS = {
     # name: ncolors, dims, precision, reunit_every, dt, sigma (A and E), bytes per link update
     "su3_fp32_128": dict(nc=3, dims=(128, 128, 128), prec="f32", reunit=10, dt=0.05, sigma=0.2, bpl=208,
                          label="SU(3) pure Yang-Mills leapfrog, 128^3 periodic, dt=0.05, FP32 links/E, "
-                               "reunitarisation every 10 steps, FP64 compensated reductions"),
+                               "reunitarisation every 10 steps, reductions accumulated in FP64"),
     "su3_fp32_96": dict(nc=3, dims=(96, 96, 96), prec="f32", reunit=10, dt=0.05, sigma=0.2, bpl=208,
                         label="SU(3) pure Yang-Mills leapfrog, 96^3 periodic (profiling size), FP32"),
     "su3_fp64_128": dict(nc=3, dims=(128, 128, 128), prec="f64", reunit=0, dt=0.05, sigma=0.2, bpl=416,

