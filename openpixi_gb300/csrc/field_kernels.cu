@@ -247,7 +247,7 @@ static void update_grid_su3f_pair_i(Ctx &c, bool reunit) {
 
 static void update_grid_su3f_pair(Ctx &c, bool reunit) {
     // 32-bit offsets while the largest link offset (3 blocks x 576 floats) fits
-    if (link_elems(c.L.V, 18) < (1L << 31) - 64) update_grid_su3f_pair_i<int>(c, reunit);
+    if (c.int_offsets) update_grid_su3f_pair_i<int>(c, reunit);
     else update_grid_su3f_pair_i<long>(c, reunit);
 }
 

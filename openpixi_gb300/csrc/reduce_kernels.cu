@@ -302,7 +302,7 @@ template <int NC, typename R>
 static void bulk_t(Ctx &c, int skip_u) {
     int nb = c.red_blocks;
     if (NC == 3 && sizeof(R) == 4 && c.pair_kernel) {
-        if (link_elems(c.L.V, 18) < (1L << 31) - 64) {
+        if (c.int_offsets) {
             static const int wave = resident_blocks(k_bulk_partial_su3f_pair<int>);
             nb = std::min(nb, wave);
             k_bulk_partial_su3f_pair<int><<<nb, RED_THREADS, 0, c.stream>>>(
