@@ -499,22 +499,50 @@ int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count) {
     if (!host_out || count != (size_t)c.L.V) { c.err = "opx_energy_density: output must hold V doubles"; return OPX_ERR_INVALID; }
     int rc = ensure_staging(c, c.L.V);
     if (rc) return rc;
+    phase_begin(c);
     launch_energy_density(c, c.staging);
     cudaMemcpyAsync(host_out, c.staging, sizeof(double) * c.L.V, cudaMemcpyDeviceToHost, c.stream);
-    return sync_check(c, "opx_energy_density");
+    rc = sync_check(c, "opx_energy_density");
+    phase_end(c, OPX_PHASE_DIA);
+    return rc;
 }
 
 int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) {
     API_CHECK_RO(ctx);
     Ctx &c = ctx->c;
     if (dir < 0 || dir > 2) { c.err = "opx_projected_energy: dir must be 0, 1 or 2"; return OPX_ERR_INVALID; }
-    const size_t n = 4 * (size_t)c.L.n[dir];
+    const int ns = c.L.n[dir];
+    const size_t n = 4 * (size_t)ns;
     if (!host_out || count != n) { c.err = "opx_projected_energy: output must hold 4*dims[dir] doubles"; return OPX_ERR_INVALID; }
-    int rc = ensure_staging(c, n);
+    int rc = ensure_staging(c, 6 * (size_t)ns);
     if (rc) return rc;
-    launch_projected_energy(c, dir, c.staging);
-    cudaMemcpyAsync(host_out, c.staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
-    return sync_check(c, "opx_projected_energy");
+    // as in opx_reduce: after one opx_step(ctx, 1) since the last call for this
+    // direction, the magnetic rows of U are that call's rows of Unext
+    auto &pc = c.pcache[dir];
+    const bool reuse = pc.calls >= 0 && c.api_calls == pc.calls + 1 && c.step1_call == c.api_calls &&
+                       c.steps == pc.steps + 1 && c.U == pc.unext;
+    pc.calls = -1;
+    std::vector<double> rows(6 * (size_t)ns);
+    phase_begin(c);
+    launch_projected_energy(c, dir, reuse ? 1 : 0, c.staging);
+    cudaMemcpyAsync(rows.data(), c.staging, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, c.stream);
+    rc = sync_check(c, "opx_projected_energy");
+    phase_end(c, OPX_PHASE_DIA);
+    if (rc) return rc;
+    for (int k = 0; k < ns; k++) {
+        // magnetic T and L of U: this call's rows, or the last call's Unext rows
+        const double tu = reuse ? pc.mag_next[k] : rows[ns + k];
+        const double lu = reuse ? pc.mag_next[ns + k] : rows[3 * (size_t)ns + k];
+        host_out[k] = rows[k];                                    // T_el
+        host_out[ns + k] = tu + rows[4 * (size_t)ns + k];         // T_mag
+        host_out[2 * (size_t)ns + k] = rows[2 * (size_t)ns + k];  // L_el
+        host_out[3 * (size_t)ns + k] = lu + rows[5 * (size_t)ns + k];  // L_mag
+    }
+    pc.mag_next.assign(rows.begin() + 4 * (size_t)ns, rows.end());
+    pc.calls = c.api_calls;
+    pc.steps = c.steps;
+    pc.unext = c.Unext;
+    return OPX_OK;
 }
 
 int opx_projected_poynting(opx_ctx *ctx, int dir, double *host_out, size_t count) {
@@ -542,9 +570,12 @@ int opx_gauss_field(opx_ctx *ctx, double *host_out, size_t count) {
     if (!host_out || count != n) { c.err = "opx_gauss_field: output must hold V*ngen doubles"; return OPX_ERR_INVALID; }
     int rc = ensure_staging(c, n);
     if (rc) return rc;
+    phase_begin(c);
     launch_gauss_field(c, c.staging);
     cudaMemcpyAsync(host_out, c.staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
-    return sync_check(c, "opx_gauss_field");
+    rc = sync_check(c, "opx_gauss_field");
+    phase_end(c, OPX_PHASE_DIA);
+    return rc;
 }
 
 int opx_particles_upload(opx_ctx *ctx, const opx_particles *p) {

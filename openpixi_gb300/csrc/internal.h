@@ -85,6 +85,13 @@ struct Ctx {
         const void *unext = nullptr;
         double bn[3] = {0, 0, 0};  // B^2 of Unext, per direction, summed over the sites
     } bcache;
+    // the same for ProjectedEnergyDensity, per direction: the Unext magnetic
+    // rows (T then L, dims[dir] each) of the last call
+    struct {
+        long calls = -1, steps = -1;
+        const void *unext = nullptr;
+        std::vector<double> mag_next;
+    } pcache[3];
     Particles P;
     // field solver: FastTYMSolver (imp_solver false) or ImplicitTYMSolver
     bool imp_solver = false;
@@ -111,7 +118,9 @@ constexpr int BULK_COLUMNS = 11;
 void launch_bulk(Ctx &c, int skip_u);
 int reduction_blocks(long V);
 void launch_energy_density(Ctx &c, double *dev_out);
-void launch_projected_energy(Ctx &c, int dir, double *dev_out);
+// six rows of dims[dir]: T_el, T_mag(U), L_el, L_mag(U), T_mag(Unext), L_mag(Unext)
+// (the U rows zero with skip_u)
+void launch_projected_energy(Ctx &c, int dir, int skip_u, double *dev_out);
 int launch_projected_poynting(Ctx &c, int dir, double *dev_out);  // SU(2) only
 void launch_gauss_field(Ctx &c, double *dev_out);
 // ---- conversions (convert_kernels.cu) ----

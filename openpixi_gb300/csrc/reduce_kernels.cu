@@ -364,12 +364,15 @@ __global__ void k_energy_density(const R *__restrict__ U, const R *__restrict__ 
 }
 
 // Block (k, part) sums slice x_dir = k over its share of the transverse sites;
-// four sums T_el, T_mag, L_el, L_mag per block, combined per slice in a fixed
-// order by k_projected_final.
+// six sums per block (PROJ_COLUMNS): T_el, T_mag of U, L_el, L_mag of U, T_mag
+// of Unext, L_mag of Unext, combined per slice in a fixed order by
+// k_projected_final.  The magnetic sums of U and Unext stay apart so that a
+// call after one step can take U's from the previous call's Unext (skip_u).
+constexpr int PROJ_COLUMNS = 6;
 template <int NC, typename R>
 __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     k_projected_energy(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
-                       const uint8_t *__restrict__ eval, Lat L, int dir, double *__restrict__ part) {
+                       const uint8_t *__restrict__ eval, Lat L, int dir, int skip_u, double *__restrict__ part) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
@@ -378,7 +381,9 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     const int o1 = (dir + 1) % 3, o2 = (dir + 2) % 3;
     const long nt = L.V / L.n[dir];
     const double area = (double)L.V / (double)L.n[dir];
-    KSum acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    KSum acc[PROJ_COLUMNS];
+#pragma unroll
+    for (int q = 0; q < PROJ_COLUMNS; q++) acc[q] = KSum{0.0, 0.0};
     for (long t = (long)blockIdx.y * blockDim.x + threadIdx.x; t < nt; t += (long)nsplit * blockDim.x) {
         int x[3];
         x[dir] = k;
@@ -388,39 +393,48 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
         const long s = x[0] * L.stride[0] + x[1] * L.stride[1] + x[2];
         if (eval && !eval[s]) continue;
         const Nbr nb = neighbours(L, s, x);
-        double el_t = 0, el_l = 0, mg_t = 0, mg_l = 0;
+        double el_t = 0, el_l = 0, mu_t = 0, mu_l = 0, mn_t = 0, mn_l = 0;
 #pragma unroll 1
         for (int j = 0; j < 3; j++) {
             const double uf = 1.0 / ((L.g * L.a[j]) * (L.g * L.a[j])) / area;
             R e[NA], b0[NA], b1[NA];
             Ep.load_ro(j, s, e);
-            field_b<G, R>(Up, L, s, nb, j, b0);
+            double mu = 0.0;
+            if (!skip_u) {
+                field_b<G, R>(Up, L, s, nb, j, b0);
+                mu = 0.25 * sqr<R, NA>(b0) * uf;
+            }
             field_b<G, R>(Unp, L, s, nb, j, b1);
             const double el = 0.5 * sqr<R, NA>(e) * uf;
-            const double mg = 0.25 * (sqr<R, NA>(b0) + sqr<R, NA>(b1)) * uf;
-            if (j == dir) { el_l += el; mg_l += mg; } else { el_t += el; mg_t += mg; }
+            const double mn = 0.25 * sqr<R, NA>(b1) * uf;
+            if (j == dir) { el_l += el; mu_l += mu; mn_l += mn; } else { el_t += el; mu_t += mu; mn_t += mn; }
         }
         two_sum_add(acc[0], el_t);
-        two_sum_add(acc[1], mg_t);
         two_sum_add(acc[2], el_l);
-        two_sum_add(acc[3], mg_l);
+        two_sum_add(acc[4], mn_t);
+        two_sum_add(acc[5], mn_l);
+        if (!skip_u) {
+            two_sum_add(acc[1], mu_t);
+            two_sum_add(acc[3], mu_l);
+        }
     }
     int q;
-    KSum v = block_reduce<4>(acc, q);
+    KSum v = block_reduce<PROJ_COLUMNS>(acc, q);
     if (q >= 0) {
-        const long o = (((long)k * nsplit + blockIdx.y) * 4 + q) * 2;
+        const long o = (((long)k * nsplit + blockIdx.y) * PROJ_COLUMNS + q) * 2;
         part[o] = v.s;
         part[o + 1] = v.c;
     }
 }
 
+// out[q][k] for the six columns of slice k
 __global__ void k_projected_final(const double *__restrict__ part, int nslices, int nsplit, double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = q * nslices + k
-    if (i >= 4 * nslices) return;
+    if (i >= PROJ_COLUMNS * nslices) return;
     const int q = i / nslices, k = i % nslices;
     KSum v{0.0, 0.0};
     for (int b = 0; b < nsplit; b++) {
-        const long o = (((long)k * nsplit + b) * 4 + q) * 2;
+        const long o = (((long)k * nsplit + b) * PROJ_COLUMNS + q) * 2;
         ksum_merge(v, KSum{part[o], part[o + 1]});
     }
     out[(long)q * nslices + k] = v.s + v.c;
@@ -603,19 +617,24 @@ static void energy_density_t(Ctx &c, double *out) {
 void launch_energy_density(Ctx &c, double *out) { OPX_DISPATCH(energy_density_t, c, out); }
 
 template <int NC, typename R>
-static void projected_energy_t(Ctx &c, int dir, double *out) {
-    // split each slice over enough blocks to fill the GPU, within the partial buffer
+static void projected_energy_t(Ctx &c, int dir, int skip_u, double *out) {
+    // split each slice over enough blocks to fill the GPU, within the partial
+    // buffer (2 * BULK_COLUMNS * max(red_blocks, 2 (n0 + n1 + n2)) doubles; 12
+    // doubles per (slice, split))
     const int ns = c.L.n[dir];
     const long nt = c.L.V / ns;
+    const long cap = 2L * BULK_COLUMNS * std::max(c.red_blocks, 2 * c.L.n[0] + 2 * c.L.n[1] + 2 * c.L.n[2]);
     int nsplit = (int)std::max<long>(1, std::min<long>(c.red_blocks / ns, nt / RED_THREADS));
-    nsplit = std::min(nsplit, (int)(c.red_blocks * 2 / ns));  // 8 doubles per (slice, split) in 16 * red_blocks
+    nsplit = (int)std::min<long>(nsplit, cap / (2L * PROJ_COLUMNS * ns));
     nsplit = std::max(nsplit, 1);
     k_projected_energy<NC, R><<<dim3(ns, nsplit), RED_THREADS, 0, c.stream>>>(
-        (const R *)c.U, (const R *)c.Unext, (const R *)c.E, c.eval, c.L, dir, c.red_part);
-    k_projected_final<<<grid_for(4L * ns, 128), 128, 0, c.stream>>>(c.red_part, ns, nsplit, out);
+        (const R *)c.U, (const R *)c.Unext, (const R *)c.E, c.eval, c.L, dir, skip_u, c.red_part);
+    k_projected_final<<<grid_for((long)PROJ_COLUMNS * ns, 128), 128, 0, c.stream>>>(c.red_part, ns, nsplit, out);
     c.launches += 2;
 }
-void launch_projected_energy(Ctx &c, int dir, double *out) { OPX_DISPATCH(projected_energy_t, c, dir, out); }
+void launch_projected_energy(Ctx &c, int dir, int skip_u, double *out) {
+    OPX_DISPATCH(projected_energy_t, c, dir, skip_u, out);
+}
 
 template <int NC, typename R>
 static void gauss_field_t(Ctx &c, double *out) {

@@ -95,3 +95,35 @@ def test_reuse_disabled_by_other_calls(native):
     b.step(3)
     b.set_evaluatable(np.ones(b.V, dtype=np.uint8))
     assert np.array_equal(vec(a.reduce()), vec(b.reduce()))
+
+
+@pytest.mark.parametrize("nc,dims,prec", [(2, (12, 8, 10), N.OPX_F64), (3, (8, 10, 6), N.OPX_F32)])
+def test_projected_energy_reuse_bit_identical(native, orc, nc, dims, prec):
+    """ProjectedEnergyDensity after one step takes the magnetic rows of U from the
+    previous call's Unext rows (per direction), interleaved with BulkQuantities
+    as a per-step diagnostics loop does; bit-identical to the recomputing twin,
+    and the FP64 rows match the oracle."""
+    g, (a, b) = twin_handles(nc, dims, prec, 0, 5, 0.3)
+    ones = np.ones(a.V, dtype=np.uint8)
+    for h in (a, b):
+        h.reduce()
+        h.projected_energy(0)
+        h.projected_energy(2)
+    for k in range(6):
+        a.step(1)
+        b.step(1)
+        b.set_evaluatable(ones)
+        oa, ob = a.reduce(), b.reduce()
+        assert np.array_equal(vec(oa), vec(ob))
+        for d in (0, 2):
+            pa, pb = a.projected_energy(d), b.projected_energy(d)
+            assert np.array_equal(pa, pb), (k, d)
+    if prec == N.OPX_F64:
+        sim = orc.OracleSimulation(g)
+        sim.initialize()
+        for _ in range(6):
+            sim.step()
+        for d in (0, 2):
+            ref = g.projected_energy(d)
+            got = a.projected_energy(d)
+            assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), d
