@@ -124,7 +124,8 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     c.na_ref = c.nc == 3 ? 9 : 3;
     c.prec = cfg->precision;
     c.pair_kernel = std::getenv("OPX_ONE_SITE_FP32") == nullptr;
-    c.int_offsets = std::getenv("OPX_LONG_OFFSETS") == nullptr && link_elems(V, 18) < (1L << 31) - 64;
+    c.int_offsets = std::getenv("OPX_LONG_OFFSETS") == nullptr && link_elems(V, c.ng) < (1L << 31) - 64 &&
+                    3L * c.na * V < (1L << 31);
     c.rsize = c.prec == OPX_F64 ? 8 : 4;
     bool ok = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) == cudaSuccess;
     auto al = [&](void **p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) { ok = false; *p = nullptr; } };

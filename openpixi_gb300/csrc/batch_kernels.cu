@@ -39,7 +39,8 @@ template <typename R> struct BEvent {
 
 // Step k of a launch starting with U = B[cur] reads B[cur ^ ((k + 1) & 1)] (the
 // links after storeFields) and writes B[cur ^ (k & 1)] (Unext).
-template <int NC, typename R>
+// I is the type of the site and element offsets (int when every event's fit).
+template <int NC, typename R, typename I>
 __global__ void __launch_bounds__(256) k_batch_persistent(const BEvent<R> *__restrict__ ev,
                                                           const int *__restrict__ list,
                                                           const int *__restrict__ begin, int nsteps, int cur,
@@ -49,8 +50,8 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BEvent<R> *__res
     const unsigned rank = cluster.block_rank();
     const int cid = blockIdx.x / csize;
     const int e0 = begin[cid], e1 = begin[cid + 1];
-    const long first = (long)rank * blockDim.x + threadIdx.x;
-    const long stride = (long)csize * blockDim.x;
+    const I first = (I)rank * (I)blockDim.x + (I)threadIdx.x;
+    const I stride = (I)csize * (I)blockDim.x;
     for (int k = 0; k < nsteps; k++) {
         const bool reunit = reunit_every > 0 && ((step0 + k + 1) % reunit_every) == 0;
         const int rd = cur ^ ((k + 1) & 1), wr = cur ^ (k & 1);
@@ -58,9 +59,9 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BEvent<R> *__res
             const BEvent<R> &e = ev[list[q]];
             const R *U = e.B[rd];
             R *Un = e.B[wr];
-            for (long s = first; s < e.L.V; s += stride) {
-                if (reunit) update_site<NC, R, false, true>(U, e.E, nullptr, Un, e.L, s);
-                else update_site<NC, R, false, false>(U, e.E, nullptr, Un, e.L, s);
+            for (I s = first; s < (I)e.L.V; s += stride) {
+                if (reunit) update_site<NC, R, false, true, I>(U, e.E, nullptr, Un, e.L, s);
+                else update_site<NC, R, false, false, I>(U, e.E, nullptr, Un, e.L, s);
             }
         }
         cluster.sync();
@@ -125,6 +126,7 @@ struct Batch {
     double *red_part = nullptr, *red_out = nullptr, *red_host = nullptr;
     std::string err;
     long launches = 0;
+    bool int_offsets = true;  // every event's link and E offsets fit in 32 bits
 };
 
 }  // namespace opx
@@ -217,9 +219,14 @@ static cudaError_t launch_persistent(Batch &b, int nsteps, cudaStream_t st) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     b.launches++;
-    return cudaLaunchKernelEx(&cfg, k_batch_persistent<NC, R>, (const BEvent<R> *)b.ev_dev,
-                              (const int *)b.list_dev, (const int *)b.begin_dev, nsteps, b.cur,
-                              b.reunit_every > 0 ? b.steps % b.reunit_every : 0L, b.reunit_every);
+    const long step0 = b.reunit_every > 0 ? b.steps % b.reunit_every : 0L;
+    if (b.int_offsets)
+        return cudaLaunchKernelEx(&cfg, k_batch_persistent<NC, R, int>, (const BEvent<R> *)b.ev_dev,
+                                  (const int *)b.list_dev, (const int *)b.begin_dev, nsteps, b.cur, step0,
+                                  b.reunit_every);
+    return cudaLaunchKernelEx(&cfg, k_batch_persistent<NC, R, long>, (const BEvent<R> *)b.ev_dev,
+                              (const int *)b.list_dev, (const int *)b.begin_dev, nsteps, b.cur, step0,
+                              b.reunit_every);
 }
 
 template <int NC, typename R>
@@ -235,7 +242,8 @@ static int max_clusters(Batch &b, int cluster, int block) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, (void *)k_batch_persistent<NC, R>, &cfg) != cudaSuccess) {
+    void *k = b.int_offsets ? (void *)k_batch_persistent<NC, R, int> : (void *)k_batch_persistent<NC, R, long>;
+    if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -294,6 +302,7 @@ int opx_batch_create(int ncolors, int nevents, const int *dims, const double *a,
         Lat L = make_lat(dims + 3 * q, aa, dt, g);
         if (L.V * 4 > 2147483647L) { delete h; return OPX_ERR_INVALID; }
         b.lats.push_back(L);
+        if (!(link_elems(L.V, b.ng) < (1L << 31) - 64 && 3L * b.na * L.V < (1L << 31))) b.int_offsets = false;
         const size_t nU = (size_t)link_elems(L.V, b.ng) * rs, nE = (size_t)L.V * 3 * b.na * rs;
         b.offB0.push_back(off); off = align256(off + nU);
         b.offB1.push_back(off); off = align256(off + nU);

@@ -24,14 +24,14 @@ int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 template <int NC, typename R> struct UpdateBounds { static constexpr int minb = 4; };
 template <> struct UpdateBounds<3, double> { static constexpr int minb = 3; };
 
-template <int NC, typename R, bool HAS_J, bool REUNIT>
+template <int NC, typename R, bool HAS_J, bool REUNIT, typename I>
 __global__ void __launch_bounds__(128, UpdateBounds<NC, R>::minb)
 k_update_grid(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ J, R *__restrict__ Unext,
               const uint8_t *__restrict__ active, Lat L) {
-    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= L.V) return;
+    const I s = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+    if (s >= (I)L.V) return;
     if (active && !active[s]) return;  // Cell.isActive gate (FastTYMSolver.java:51)
-    update_site<NC, R, HAS_J, REUNIT>(U, E, J, Unext, L, s);
+    update_site<NC, R, HAS_J, REUNIT, I>(U, E, J, Unext, L, s);
 }
 
 // SU(3) FP32: two sites per thread in paired FP32 instructions.  Warp w
@@ -182,8 +182,8 @@ static int implicit_update_t(Ctx &c) {
     // ImplicitBegin (:68-90): the explicit combined update into the implicit grid
     const int B = 128;
     const dim3 grid(grid_for(V, B));
-    if (c.j_nonzero) k_update_grid<2, R, true, false><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
-    else k_update_grid<2, R, false, false><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
+    if (c.j_nonzero) k_update_grid<2, R, true, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
+    else k_update_grid<2, R, false, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
     c.launches++;
     for (int it = 0; it < c.imp_iterations; it++) {
         std::swap(Ui, Uin);  // implicitGrid.storeFields()
@@ -251,6 +251,17 @@ static void update_grid_su3f_pair(Ctx &c, bool reunit) {
     else update_grid_su3f_pair_i<long>(c, reunit);
 }
 
+template <int NC, typename R, typename I>
+static void launch_update_grid_i(Ctx &c, bool reunit, dim3 grid, int B, const R *U, R *E, const R *J, R *Un) {
+    if (c.j_nonzero) {
+        if (reunit) k_update_grid<NC, R, true, true, I><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+        else k_update_grid<NC, R, true, false, I><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+    } else {
+        if (reunit) k_update_grid<NC, R, false, true, I><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+        else k_update_grid<NC, R, false, false, I><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
+    }
+}
+
 template <int NC, typename R>
 static void update_grid_t(Ctx &c, bool reunit) {
     if (NC == 3 && sizeof(R) == 4 && c.pair_kernel) {
@@ -262,13 +273,8 @@ static void update_grid_t(Ctx &c, bool reunit) {
     const R *U = (const R *)c.U;
     R *E = (R *)c.E, *Un = (R *)c.Unext;
     const R *J = (const R *)c.J;
-    if (c.j_nonzero) {
-        if (reunit) k_update_grid<NC, R, true, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
-        else k_update_grid<NC, R, true, false><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
-    } else {
-        if (reunit) k_update_grid<NC, R, false, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
-        else k_update_grid<NC, R, false, false><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
-    }
+    if (c.int_offsets) launch_update_grid_i<NC, R, int>(c, reunit, grid, B, U, E, J, Un);
+    else launch_update_grid_i<NC, R, long>(c, reunit, grid, B, U, E, J, Un);
     c.launches++;
 }
 

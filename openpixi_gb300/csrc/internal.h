@@ -56,9 +56,9 @@ struct Ctx {
     // instructions (environment OPX_ONE_SITE_FP32=1 selects the
     // one-site-per-thread forms)
     bool pair_kernel = true;
-    // 32-bit element offsets in the paired kernels while every link offset fits
-    // (54 V < 2^31); OPX_LONG_OFFSETS=1 selects the 64-bit forms at any size, so
-    // that tests can compare them on small lattices
+    // 32-bit site and element offsets in the leapfrog kernels while every link
+    // and E offset fits (SU(3): 54 V < 2^31); OPX_LONG_OFFSETS=1 selects the
+    // 64-bit forms at any size, so that tests can compare them on small lattices
     bool int_offsets = true;
     double *staging = nullptr;
     size_t staging_len = 0;  // doubles

@@ -2,11 +2,13 @@
 //
 // Site index s = ((x0*N1)+x1)*N2+x2, dimension 0 slowest (Grid.java:757-770),
 // so dimension 2 is contiguous and a warp reads 32 consecutive sites.
-// Links are stored in warp-sized blocks of 32 consecutive sites,
-//   U[d][s/32][c][s%32]   (c < NG: 4 for SU(2), 18 for SU(3)),
+// SU(3) links are stored in warp-sized blocks of 32 consecutive sites,
+//   U[d][s/32][c][s%32]   (c < 18),
 // so that component c of 32 consecutive sites is one 128-byte (FP32) or
-// 256-byte (FP64) line, and the NG components of one link sit at fixed
+// 256-byte (FP64) line, and the 18 components of one link sit at fixed
 // 32-element strides from one address (one address computation per link).
+// SU(2) links keep their four quaternion components together, U[d][s][4]
+// (one vector load per link), with the site count padded to 32.
 // Algebra fields are plain planes, one contiguous array of V values per
 // component:
 //   fields E[d][a][s]  (a < NA: 3 for SU(2), 8 for SU(3), generator components)
@@ -98,11 +100,14 @@ struct Nbr {
     long bwd[3];  // index of x - d
 };
 
-__device__ __forceinline__ void site_coords(const Lat &L, long s, int *x) {
-    long t = s / L.n[2];
-    x[2] = (int)(s - t * L.n[2]);
-    long u = t / L.n[1];
-    x[1] = (int)(t - u * L.n[1]);
+// Coordinates of site s; I = int where the site index fits (32-bit divisions
+// are several times cheaper than 64-bit ones).
+template <typename I>
+__device__ __forceinline__ void site_coords(const Lat &L, I s, int *x) {
+    const I t = s / (I)L.n[2];
+    x[2] = (int)(s - t * (I)L.n[2]);
+    const I u = t / (I)L.n[1];
+    x[1] = (int)(t - u * (I)L.n[1]);
     x[0] = (int)u;
 }
 
@@ -165,18 +170,24 @@ template <> __device__ __forceinline__ double ld<double>(const double *p) { retu
 // contiguous (one 16-byte vector load in FP32, two in FP64), links of
 // consecutive sites consecutive.  Both pad the site count to a multiple of 32.
 __host__ __device__ __forceinline__ long link_blocks(long V) { return (V + 31) >> 5; }
+// Element offset of component c of link (s, d); I = int where every offset fits.
+template <typename I>
+__host__ __device__ __forceinline__ I link_offset_t(I V, int NG, int d, int c, I s) {
+    const I nb = (V + 31) >> 5;
+    if (NG == 4) return ((I)d * (nb << 5) + s) * 4 + c;
+    return (((I)d * nb + (s >> 5)) * NG + c) * 32 + (s & 31);
+}
 __host__ __device__ __forceinline__ long link_offset(long V, int NG, int d, int c, long s) {
-    if (NG == 4) return ((long)d * (link_blocks(V) << 5) + s) * 4 + c;
-    return (((long)d * link_blocks(V) + (s >> 5)) * NG + c) * 32 + (s & 31);
+    return link_offset_t<long>(V, NG, d, c, s);
 }
 __host__ __device__ __forceinline__ long link_elems(long V, int NG) { return 3L * link_blocks(V) * 32 * NG; }
 
-// Structure-of-arrays views
-template <class G, typename R> struct LinkPlanes {
+// Structure-of-arrays views; I is the type of the site and element offsets.
+template <class G, typename R, typename I = long> struct LinkPlanes {
     R *p;
-    long V;
-    __device__ __forceinline__ typename G::M load(int d, long s) const;
-    __device__ __forceinline__ void store(int d, long s, const typename G::M &m) const;
+    I V;
+    __device__ __forceinline__ typename G::M load(int d, I s) const;
+    __device__ __forceinline__ void store(int d, I s, const typename G::M &m) const;
 };
 
 // Four contiguous reals: vector loads and stores for the built-in types.
@@ -203,52 +214,52 @@ template <> __device__ __forceinline__ void st4<double>(double *b, const double 
     reinterpret_cast<double2 *>(b)[1] = make_double2(e[2], e[3]);
 }
 
-template <typename R> struct LinkPlanes<SU2<R>, R> {
+template <typename R, typename I> struct LinkPlanes<SU2<R>, R, I> {
     R *p;
-    long V;
-    __device__ __forceinline__ Q2<R> load(int d, long s) const {
+    I V;
+    __device__ __forceinline__ Q2<R> load(int d, I s) const {
         Q2<R> q;
-        ld4<R>(p + link_offset(V, 4, d, 0, s), q.e);
+        ld4<R>(p + link_offset_t<I>(V, 4, d, 0, s), q.e);
         return q;
     }
-    __device__ __forceinline__ void store(int d, long s, const Q2<R> &m) const {
-        st4<R>(p + link_offset(V, 4, d, 0, s), m.e);
+    __device__ __forceinline__ void store(int d, I s, const Q2<R> &m) const {
+        st4<R>(p + link_offset_t<I>(V, 4, d, 0, s), m.e);
     }
 };
 
-template <typename R> struct LinkPlanes<SU3<R>, R> {
+template <typename R, typename I> struct LinkPlanes<SU3<R>, R, I> {
     R *p;
-    long V;
-    __device__ __forceinline__ M3<R> load(int d, long s) const {
-        const R *b = p + link_offset(V, 18, d, 0, s);
+    I V;
+    __device__ __forceinline__ M3<R> load(int d, I s) const {
+        const R *b = p + link_offset_t<I>(V, 18, d, 0, s);
         M3<R> m;
 #pragma unroll
         for (int k = 0; k < 9; k++) { m.r[k] = ld(b + k * 32); m.i[k] = ld(b + (9 + k) * 32); }
         return m;
     }
-    __device__ __forceinline__ void store(int d, long s, const M3<R> &m) const {
-        R *b = p + link_offset(V, 18, d, 0, s);
+    __device__ __forceinline__ void store(int d, I s, const M3<R> &m) const {
+        R *b = p + link_offset_t<I>(V, 18, d, 0, s);
 #pragma unroll
         for (int k = 0; k < 9; k++) { b[k * 32] = m.r[k]; b[(9 + k) * 32] = m.i[k]; }
     }
 };
 
 // Algebra-valued link field E[d][a][s] (or site field with d = 0).
-template <int NA, typename R> struct AlgPlanes {
+template <int NA, typename R, typename I = long> struct AlgPlanes {
     R *p;
-    long V;
-    __device__ __forceinline__ void load(int d, long s, R *x) const {
-        const R *b = p + (long)d * NA * V + s;
+    I V;
+    __device__ __forceinline__ void load(int d, I s, R *x) const {
+        const R *b = p + ((I)d * NA * V + s);
 #pragma unroll
         for (int a = 0; a < NA; a++) x[a] = b[a * V];
     }
-    __device__ __forceinline__ void load_ro(int d, long s, R *x) const {
-        const R *b = p + (long)d * NA * V + s;
+    __device__ __forceinline__ void load_ro(int d, I s, R *x) const {
+        const R *b = p + ((I)d * NA * V + s);
 #pragma unroll
         for (int a = 0; a < NA; a++) x[a] = ld(b + a * V);
     }
-    __device__ __forceinline__ void store(int d, long s, const R *x) const {
-        R *b = p + (long)d * NA * V + s;
+    __device__ __forceinline__ void store(int d, I s, const R *x) const {
+        R *b = p + ((I)d * NA * V + s);
 #pragma unroll
         for (int a = 0; a < NA; a++) b[a * V] = x[a];
     }

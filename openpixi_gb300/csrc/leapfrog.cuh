@@ -16,32 +16,34 @@
 
 namespace opx {
 
-template <int NC, typename R, bool HAS_J, bool REUNIT>
+// I is the type of the site and element offsets: int where they fit (the
+// 64-bit divisions and address arithmetic of long cost issue slots).
+template <int NC, typename R, bool HAS_J, bool REUNIT, typename I = long>
 __device__ __forceinline__ void update_site(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ J,
-                                            R *__restrict__ Unext, const Lat &L, long s) {
+                                            R *__restrict__ Unext, const Lat &L, I s) {
     using G = typename GroupOf<NC, R>::T;
     using M = typename G::M;
     constexpr int NA = G::NA;
     int x[3];
-    site_coords(L, s, x);
-    const Deltas<long> D = deltas<long>(L, x);
-    const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V};
-    const LinkPlanes<G, R> Un{Unext, L.V};
-    const AlgPlanes<NA, R> Ep{E, L.V};
-    const AlgPlanes<NA, R> Jp{const_cast<R *>(J), L.V};
+    site_coords<I>(L, s, x);
+    const Deltas<I> D = deltas<I>(L, x);
+    const LinkPlanes<G, R, I> Up{const_cast<R *>(U), (I)L.V};
+    const LinkPlanes<G, R, I> Un{Unext, (I)L.V};
+    const AlgPlanes<NA, R, I> Ep{E, (I)L.V};
+    const AlgPlanes<NA, R, I> Jp{const_cast<R *>(J), (I)L.V};
     const R dt = LatR<R>::dt(L);
 
 #pragma unroll 1
     for (int i = 0; i < 3; i++) {
-        const long s_pi = s + D.f(i);  // x + i
+        const I s_pi = s + D.f(i);  // x + i
         M S = G::zero();
 #pragma unroll 1
         for (int jj = 1; jj < 3; jj++) {
             const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
-            const long bj = D.b(j);
-            const long s_pj = s + D.f(j);  // x + j
-            const long s_mj = s + bj;      // x - j
-            const long s_pimj = s_pi + bj; // x + i - j
+            const I bj = D.b(j);
+            const I s_pj = s + D.f(j);  // x + j
+            const I s_mj = s + bj;      // x - j
+            const I s_pimj = s_pi + bj; // x + i - j
             // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
             M F = G::mul_adj(G::mul_adj(Up.load(j, s_pi), Up.load(i, s_pj)), Up.load(j, s));
             // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)

@@ -315,19 +315,22 @@ def test_empty_particle_list_and_oversized_lattice(native):
     h2.initialize()
 
 
-def test_fp32_su3_long_offsets_match(native):
-    """The paired SU(3) FP32 leapfrog and reduction with 64-bit element offsets
-    (the form lattices of 54 V >= 2^31 take; OPX_LONG_OFFSETS=1 selects it at
-    any size) against the 32-bit form on a small lattice: bit-identical links, E
-    and observables, with a current and with re-unitarisation steps."""
+@pytest.mark.parametrize("nc,prec", [(3, N.OPX_F32), (3, N.OPX_F64), (2, N.OPX_F32), (2, N.OPX_F64)])
+def test_long_offsets_match(native, nc, prec):
+    """The leapfrog and reduction kernels with 64-bit site and element offsets
+    (the forms lattices too large for 32-bit offsets take; OPX_LONG_OFFSETS=1
+    selects them at any size) against the 32-bit forms on a small lattice:
+    bit-identical links, E and observables, with a current and (FP32) with
+    re-unitarisation steps."""
     import os
-    g = fresh(oracle_ic(3, (7, 9, 11), 21, 0.2, 0.2))
+    g = fresh(oracle_ic(nc, (7, 9, 11), 21, 0.2, 0.2))
     rng = np.random.default_rng(8)
     g.J[...] = rng.normal(0, 0.02, g.J.shape)
-    ha = handle_from_oracle(g, precision=N.OPX_F32, reunit_every=4)
+    ru = 4 if prec == N.OPX_F32 else 0
+    ha = handle_from_oracle(g, precision=prec, reunit_every=ru)
     os.environ["OPX_LONG_OFFSETS"] = "1"
     try:
-        hb = handle_from_oracle(g, precision=N.OPX_F32, reunit_every=4)
+        hb = handle_from_oracle(g, precision=prec, reunit_every=ru)
     finally:
         os.environ.pop("OPX_LONG_OFFSETS", None)
     for h in (ha, hb):
