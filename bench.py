@@ -356,11 +356,12 @@ def bench_cgc(device, nsteps=300, oracle_steps=2):
     proj = []
     h.synchronize()
     t = time.perf_counter()
-    for _ in range(nsteps):
-        h.step(1)
-        o = h.reduce()
-        proj.append(h.projected_energy(0))
-        gmax = max(gmax, o.gauss)
+    with nvtx_range("cgc_steps"):
+        for _ in range(nsteps):
+            h.step(1)
+            o = h.reduce()
+            proj.append(h.projected_energy(0))
+            gmax = max(gmax, o.gauss)
     h.synchronize()
     wall_ms = 1000.0 * (time.perf_counter() - t)
     ms, counts = h.phase_times()
