@@ -506,15 +506,15 @@ def bench_differentiation(device, ndir=64):
 
 
 def bench_configs(device):
-    """Parity of the other single-GPU configurations at full size:
-    SU(2) FP64 32^3, 100 steps (config 1) against the oracle per link; the SU(3)
-    FP32 form against the FP64 GPU run on 128^3 x 500 steps (energy and per
-    link) and against the oracle on a 32^3 lattice of the same generator."""
+    """Parity legs at full size: the plain SU(2) FP64 workload (32^3, 100
+    steps) against the oracle per link; the SU(3) FP32 form against the FP64 GPU
+    run on 128^3 x 500 steps (energy and per link) and against the oracle on a
+    32^3 lattice of the same generator."""
     import openpixi_gb300 as opx
     from openpixi_gb300 import _native as N
     import oracle
     out = {}
-    # config 1
+    # SU(2) FP64 32^3 x 100 steps against the oracle
     g = oracle.OracleGrid(2, (32, 32, 32), dt=0.05)
     g.random_fields(SEED + 1, 0.1, 0.1)
     g.gauss_project(1e-26)
@@ -535,12 +535,12 @@ def bench_configs(device):
     eo = g.E.reshape(-1, 3)
     de = (np.linalg.norm(ev - eo, axis=1) / np.maximum(np.linalg.norm(eo, axis=1), np.sqrt((eo ** 2).sum(1).mean()))).max()
     bo, bd = g.bulk(), h.reduce()
-    out["config1_su2_fp64_32"] = {"steps": 100, "gpu_ms_per_step": ms / 100, "oracle_s_1thread": t_orc,
+    out["su2_fp64_32_parity"] = {"steps": 100, "gpu_ms_per_step": ms / 100, "oracle_s_1thread": t_orc,
                                   "max_rel_link_err": float(du), "max_rel_E_err": float(de),
                                   "energy_rel_err": abs(bd.e2_total + bd.b2_total - bo[11] - bo[12]) / (bo[11] + bo[12]),
                                   "gauss": bd.gauss, "bar": 1e-10}
     h.close()
-    # config 3: FP32 against FP64 on the full lattice, and against the oracle on 32^3
+    # SU(3) FP32 against FP64 on the full lattice, and against the oracle on 32^3
     res = {}
     for dims, nsteps, key in (((128, 128, 128), 500, "gpu_fp64_128"), ((32, 32, 32), 500, "oracle_32")):
         h64 = opx.Handle(3, dims, dt=0.05, precision=N.OPX_F64, device=device)
@@ -577,7 +577,7 @@ def bench_configs(device):
                     "max_rel_link_err": float(d.max()), "mean_rel_link_err": float(d.mean())}
         h64.close()
         h32.close()
-    out["config3_fp32_errors"] = res
+    out["su3_fp32_errors"] = res
     return out
 
 
@@ -757,7 +757,7 @@ def main():
     if rank == 0 and not args.no_configs and args.workload == "su3_fp32_128":
         try:
             configs = bench_configs(device)
-            configs["config5_differentiation"] = bench_differentiation(device)
+            configs["su2_64_differentiation"] = bench_differentiation(device)
         except Exception as e:  # the headline stands without the extra legs
             configs = {"skipped": str(e)}
 
