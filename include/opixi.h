@@ -205,6 +205,18 @@ typedef struct {
  * handles, beam along direction 0.  Call opx_initialize afterwards. */
 int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n);
 
+/* WilsonLineObservables (physics/initial/CGC/WilsonLineObservables.java:37-131)
+ * of nucleus k of the last opx_cgc_mv / opx_cgc_mv_super call, from the
+ * Poisson solver's Wilson lines V at the longitudinal boundary behind the
+ * nucleus (LightConePoissonSolverImproved.getV, :125-136, :231):
+ * computeTadpole's mean of Re tr V over the transverse cells, and
+ * computeDipole's mean of Re tr(V(x) V(y)^dagger) over all pairs of transverse
+ * cells binned by their periodic distance, (int) sqrt(n1 n2) / 2 bins of width
+ * min(n1 a1, n2 a2) / 2 / nbins (empty bins NaN, as in the reference).
+ * tadpole, dipole (nbins values) and bin_width may each be NULL. */
+int opx_cgc_wilson_lines(opx_ctx *ctx, int nucleus, double *tadpole, double *dipole, size_t nbins,
+                         double *bin_width);
+
 /* ---- occupation numbers (diagnostics/methods/OccupationNumbersInTime.java:172-297) ----
  * On copies of the handle's fields: the Coulomb gauge iteration of
  * CoulombGauge.applyGaugeTransformation (physics/gauge/CoulombGauge.java:56-194;

@@ -45,6 +45,7 @@ EXPORTED = [
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
     "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
     "opx_super_download", "opx_super_upload", "opx_occupation_numbers", "opx_set_field_solver",
+    "opx_cgc_wilson_lines",
 ]
 
 
@@ -143,6 +144,7 @@ def load(path=None):
         "opx_batch_config": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "opx_batch_kernel_launches": (C.c_long, [vp]),
         "opx_cgc_mv": (C.c_int, [vp, vp, C.c_int]),
+        "opx_cgc_wilson_lines": (C.c_int, [vp, C.c_int, dp, dp, C.c_size_t, dp]),
         "opx_particles_count": (C.c_long, [vp]),
         "opx_projected_poynting": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
         "opx_cgc_mv_super": (C.c_int, [vp, vp, C.c_int]),
@@ -336,6 +338,19 @@ class Handle:
                 setattr(arr[k], f, nu[f])
         self.check(self.L.opx_cgc_mv(self.h, arr, len(nuclei)))
         self.np = self.L.opx_particles_count(self.h)
+
+    def cgc_wilson_lines(self, nucleus=0, dipole=True):
+        """WilsonLineObservables of nucleus k of the last CGC call: (tadpole,
+        dipole bins or None, bin width)."""
+        import math
+        n1, n2 = self.dims[1], self.dims[2]
+        nb = int(math.sqrt(n1 * n2)) // 2  # (int) Math.sqrt(totalCells) / 2
+        t, w = C.c_double(), C.c_double()
+        d = np.empty(nb) if dipole else None
+        self.check(self.L.opx_cgc_wilson_lines(self.h, int(nucleus), C.byref(t),
+                                               None if d is None else d.ctypes.data_as(C.POINTER(C.c_double)),
+                                               nb if dipole else 0, C.byref(w)))
+        return t.value, d, w.value
 
     def set_field_solver(self, kind, iterations=0, damping=0.0):
         """FastTYMSolver (SOLVER_FAST) or ImplicitTYMSolver(iterations, damping) (SOLVER_IMPLICIT)."""

@@ -4,7 +4,9 @@
 and ``CGCInitialCondition`` follows CGCInitialCondition.applyInitialCondition
 (:55-93): charges, the improved light-cone Poisson solver
 (LightConePoissonSolverImproved) and the NGP particle creator
-(LightConeNGPParticleCreator), all done by ``opx_cgc_mv`` on the device.
+(LightConeNGPParticleCreator), all done by ``opx_cgc_mv`` on the device; the
+optional Wilson-line tadpole and dipole (WilsonLineObservables) by
+``opx_cgc_wilson_lines``.
 YAML: ``initialConditions: CGC: {poissonSolver, MVModel: [...]}``
 (ui/util/yaml/initial/YamlCGC.java, YamlMVModel.java).
 """
@@ -52,6 +54,8 @@ class CGCInitialCondition:
         self.setPoissonSolver(poissonSolver)
         self.computeTadpole = False
         self.computeDipole = False
+        self.tadpoleFilename = "tadpole.txt"
+        self.dipoleFilename = "dipole.txt"
 
     def setInitialChargeDensity(self, rho):
         self.initialChargeDensity = rho
@@ -69,8 +73,6 @@ class CGCInitialCondition:
         if s.simulationType not in ("TemporalCGCNGP", "TemporalImplicitCGCNGP", "TemporalOptimizedCGCNGP",
                                     "TemporalOptimizedImplicitCGCNGP"):
             raise RuntimeError("CGCInitialCondition: simulation type not supported!")
-        if self.computeTadpole or self.computeDipole:
-            raise NotImplementedError("Wilson line observables (tadpole, dipole) are not provided")
         h = s.grid.handle
         if s.simulationType in SUPER_PARTICLES:
             # LightConeNGPSuperParticleCreator: CGCSuperParticle groups
@@ -80,7 +82,27 @@ class CGCInitialCondition:
             # LightConeNGPParticleCreator: CGCParticle list
             h.cgc_mv([self.initialChargeDensity.as_nucleus()])
             s.particles = h.np
+        if self.computeTadpole or self.computeDipole:
+            self._wilson_line_observables(h, s)
         s.grid._dirty()
+
+    def _wilson_line_observables(self, h, s):
+        """WilsonLineObservables.computeTadpole / computeDipole
+        (physics/initial/CGC/WilsonLineObservables.java:37-131), appended to the
+        files in the reference's format (FileFunctions.getFile: relative paths
+        go under output/)."""
+        from .diagnostics import java_sci
+        tadpole, dipole, ds = h.cgc_wilson_lines(0, dipole=self.computeDipole)
+        info = self.initialChargeDensity.getInfo()
+        if self.computeTadpole:
+            with open(_output_file(self.tadpoleFilename), "a") as f:
+                f.write(info + ", V: " + java_sci(tadpole) + "\n")
+        if self.computeDipole:
+            with open(_output_file(self.dipoleFilename), "a") as f:
+                f.write(info + "\n")
+                f.write("d\ttr(V V^t)\n")
+                for b, v in enumerate(dipole):
+                    f.write(java_sci(b * ds) + "\t" + java_sci(v) + "\n")
 
     @staticmethod
     def from_yaml(cgc):
@@ -98,8 +120,19 @@ class CGCInitialCondition:
             ic = CGCInitialCondition(rho, cgc.get("poissonSolver"))
             ic.computeTadpole = bool(cgc.get("computeTadpole", False))
             ic.computeDipole = bool(cgc.get("computeDipole", False))
+            ic.tadpoleFilename = cgc.get("tadpoleFilename", "tadpole.txt")
+            ic.dipoleFilename = cgc.get("dipoleFilename", "dipole.txt")
             out.append(ic)
         return out
+
+
+def _output_file(path):
+    """FileFunctions.getFile (diagnostics/FileFunctions.java:16-32): relative
+    paths are prefixed with output/, and the parent folder is created."""
+    import os
+    p = path if path.startswith("/") else os.path.join("output", path)
+    os.makedirs(os.path.dirname(p) or ".", exist_ok=True)
+    return p
 
 
 __all__ = ["MVModel", "CGCInitialCondition"]

@@ -78,6 +78,7 @@ static void fill_identity(Ctx &c, void *U) {
 static void release(Ctx &c) {
     cpic_free(c);
     super_free(c);
+    cgc_vt_free(c);
     void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.red_count, c.status,
                    c.imp_Ua, c.imp_Ub, c.imp_E};
     for (void *p : dev) if (p) cudaFree(p);

@@ -24,6 +24,7 @@
 // reference assumes it too).
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -35,6 +36,7 @@
 #include "fftlib.h"
 #include "internal.h"
 #include "java_random.h"
+#include "ksum.cuh"
 
 namespace opx {
 
@@ -422,6 +424,107 @@ using namespace opx;
 
 
 // Host driver; returns the particles created for this nucleus (reference layout, host).
+// ---- Wilson-line observables (physics/initial/CGC/WilsonLineObservables.java) ----
+
+__device__ __forceinline__ void put_ref(const Q2<double> &m, double *o) {
+    for (int k = 0; k < 4; k++) o[k] = m.e[k];
+}
+__device__ __forceinline__ void put_ref(const M3<double> &m, double *o) {
+    for (int k = 0; k < 9; k++) { o[k] = m.r[k]; o[9 + k] = m.i[k]; }
+}
+// Re tr V (GroupElement.getRealTrace) and Re tr(A B^dagger) of reference-layout elements
+template <int NC> __device__ __forceinline__ double retr(const double *a) {
+    return NC == 2 ? 2.0 * a[0] : a[0] + a[4] + a[8];
+}
+template <int NC> __device__ __forceinline__ double retr_adj(const double *a, const double *b) {
+    double s = 0.0;
+    for (int k = 0; k < (NC == 2 ? 4 : 18); k++) s = fma(a[k], b[k], s);
+    return NC == 2 ? 2.0 * s : s;
+}
+
+// VT: V at the longitudinal boundary behind the nucleus, z = 0 for orientation
+// +1 and n0 - 1 for -1 (LightConePoissonSolverImproved.solve :125-136), taken
+// before the improved links modify V
+template <int NC>
+__global__ void k_extract_vt(const double *__restrict__ Vl, double *__restrict__ vt, long V, long ntr, int zb) {
+    using G = typename GroupOf<NC, double>::T;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntr) return;
+    const LinkPlanes<G, double> Vp{const_cast<double *>(Vl), V};
+    put_ref(Vp.load(0, (long)zb * ntr + t), vt + t * G::NG);
+}
+
+// WilsonLineObservables.computeTadpole (:37-59): one block, cells strided over
+// the threads, a fixed-order block sum
+template <int NC>
+__global__ void k_tadpole(const double *__restrict__ vt, long ntr, double *__restrict__ out) {
+    constexpr int NG = NC == 2 ? 4 : 18;
+    KSum acc[1] = {{0.0, 0.0}};
+    for (long t = threadIdx.x; t < ntr; t += blockDim.x) two_sum_add(acc[0], retr<NC>(vt + t * NG));
+    int q;
+    const KSum v = block_reduce<1>(acc, q);
+    if (q == 0) out[0] = (v.s + v.c) / (double)ntr;
+}
+
+// WilsonLineObservables.computeDipole (:67-131): block i takes cell x_i against
+// every cell y (threads stride over y); Re tr(V(x) V(y)^dagger) goes to the bin
+// of the periodic transverse distance, exactly as the reference forms it
+// (integer coordinate differences wrapped at n/2, sqrt, truncation by ds).
+// Each thread keeps its own column of bins in shared memory; the block adds the
+// columns in order into part[i][bin], and k_dipole_final adds the cells in order.
+template <int NC>
+__global__ void k_dipole(const double *__restrict__ vt, int n1, int n2, double a1, double a2, int nb, double ds,
+                         double *__restrict__ part, long long *__restrict__ cnt) {
+    constexpr int NG = NC == 2 ? 4 : 18;
+    extern __shared__ double dsh[];  // [nb][blockDim] sums, then [nb][blockDim] counts
+    const int B = blockDim.x, tid = threadIdx.x;
+    double *sum = dsh;
+    long long *num = reinterpret_cast<long long *>(dsh + (size_t)nb * B);
+    for (int b = 0; b < nb; b++) { sum[b * B + tid] = 0.0; num[b * B + tid] = 0; }
+    const long ntr = (long)n1 * n2, i = blockIdx.x;
+    const int x0 = (int)(i / n2), x1 = (int)(i % n2);
+    double vi[NG];
+    for (int k = 0; k < NG; k++) vi[k] = vt[i * NG + k];
+    for (long j = tid; j < ntr; j += B) {
+        const int y0 = (int)(j / n2), y1 = (int)(j % n2);
+        double d0 = fabs((double)(x0 - y0)), d1 = fabs((double)(x1 - y1));
+        if (d0 > n1 / 2) d0 -= n1;
+        if (d1 > n2 / 2) d1 -= n2;
+        double dist = 0.0;
+        dist += d0 * d0 * a1 * a1;
+        dist += d1 * d1 * a2 * a2;
+        dist = sqrt(dist);
+        const int bin = (int)(dist / ds);
+        if (bin < nb) {
+            sum[bin * B + tid] += retr_adj<NC>(vi, vt + j * NG);
+            num[bin * B + tid] += 1;
+        }
+    }
+    __syncthreads();
+    for (int b = tid; b < nb; b += B) {
+        double s = 0.0;
+        long long c = 0;
+        for (int t = 0; t < B; t++) { s += sum[b * B + t]; c += num[b * B + t]; }
+        part[i * nb + b] = s;
+        cnt[i * nb + b] = c;
+    }
+}
+
+__global__ void k_dipole_final(const double *__restrict__ part, const long long *__restrict__ cnt, long ntr, int nb,
+                               double *__restrict__ out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    KSum v{0.0, 0.0};
+    long long c = 0;
+    for (long i = 0; i < ntr; i++) { two_sum_add(v, part[i * nb + b]); c += cnt[i * nb + b]; }
+    out[b] = (v.s + v.c) / (double)c;  // 0/0 = NaN for an empty bin, as in the reference
+}
+
+void opx::cgc_vt_free(Ctx &c) {
+    for (double *p : c.cgc_vt) if (p) cudaFree(p);
+    c.cgc_vt.clear();
+}
+
 static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &ppos0, std::vector<double> &ppos1,
                        std::vector<double> &pvel, std::vector<double> &pq, std::vector<int32_t> &pdir,
                        SuperGroup *sg) {
@@ -446,6 +549,9 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
     al((void **)&Ec, sizeof(double) * 3 * NA * V);
     al((void **)&Gv, sizeof(double) * NA * V);
     al((void **)&smax, sizeof(double) * n0);
+    double *vt = nullptr;  // kept on the handle for opx_cgc_wilson_lines
+    al((void **)&vt, sizeof(double) * ntr * c.ng);
+    if (vt) c.cgc_vt.push_back(vt);
     int rc = OPX_OK;
     FFTPlan p3, p2;
     if (ok) {
@@ -503,6 +609,7 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
         if (nc == 2) {
             k_identity0<2><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, V);
             k_wilson_scan<2><<<grid_for(ntr, 128), 128, 0, c.stream>>>(phi, Vl, n0, ntr, orientation, -L.g * aL);
+            if (vt) k_extract_vt<2><<<grid_for(ntr, 128), 128, 0, c.stream>>>(Vl, vt, V, ntr, orientation > 0 ? 0 : n0 - 1);
             k_gauge_links<2><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, (double *)c.U, Uc, L, direction);
             k_improved_w<2><<<grid_for(V, 128), 128, 0, c.stream>>>(phi, Vl, L, direction, orientation, 20);
             k_gauge_links<2><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, (double *)c.Unext, Unc, L, direction);
@@ -512,6 +619,7 @@ static int cgc_nucleus(Ctx &c, const opx_mv_nucleus &nu, std::vector<double> &pp
         } else {
             k_identity0<3><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, V);
             k_wilson_scan<3><<<grid_for(ntr, 128), 128, 0, c.stream>>>(phi, Vl, n0, ntr, orientation, -L.g * aL);
+            if (vt) k_extract_vt<3><<<grid_for(ntr, 128), 128, 0, c.stream>>>(Vl, vt, V, ntr, orientation > 0 ? 0 : n0 - 1);
             k_gauge_links<3><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, (double *)c.U, Uc, L, direction);
             k_improved_w<3><<<grid_for(V, 128), 128, 0, c.stream>>>(phi, Vl, L, direction, orientation, 20);
             k_gauge_links<3><<<grid_for(V, 128), 128, 0, c.stream>>>(Vl, (double *)c.Unext, Unc, L, direction);
@@ -627,6 +735,8 @@ extern "C" int opx_cgc_mv(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int n) {
     }
     if (!fft_lib().load(c.err)) return OPX_ERR_UNSUPPORTED;
     if (!c.sg.empty()) { c.err = "opx_cgc_mv: the handle holds super particles (optimized CGC type)"; return OPX_ERR_INVALID; }
+    cudaStreamSynchronize(c.stream);
+    cgc_vt_free(c);
     // particles already on the handle stay first in the list (s.particles.add appends)
     const long n0 = c.P.n;
     const int nar = c.na_ref;
@@ -669,6 +779,8 @@ extern "C" int opx_cgc_mv_super(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int 
     }
     std::vector<double> p0, p1, v, q0;
     std::vector<int32_t> d;
+    cudaStreamSynchronize(c.stream);
+    cgc_vt_free(c);
     for (int k = 0; k < n; k++) {
         opx_mv_nucleus nu = nuclei[k];
         if (!nu.use_seed) nu.seed = (int)std::random_device{}();
@@ -678,5 +790,70 @@ extern "C" int opx_cgc_mv_super(opx_ctx *ctx, const opx_mv_nucleus *nuclei, int 
         c.sg.push_back(G);
     }
     c.sg_ppc = ppc;
+    return OPX_OK;
+}
+
+extern "C" int opx_cgc_wilson_lines(opx_ctx *ctx, int nucleus, double *tadpole, double *dipole, size_t nbins,
+                                    double *bin_width) {
+    if (!ctx) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    if (nucleus < 0 || nucleus >= (int)c.cgc_vt.size()) {
+        c.err = "opx_cgc_wilson_lines: no such nucleus in the last CGC initial condition";
+        return OPX_ERR_INVALID;
+    }
+    const int n1 = c.L.n[1], n2 = c.L.n[2];
+    const long ntr = (long)n1 * n2;
+    const int nb = (int)std::sqrt((double)ntr) / 2;
+    if (dipole && nbins != (size_t)nb) {
+        c.err = "opx_cgc_wilson_lines: the dipole has (int) sqrt(n1 n2) / 2 = " + std::to_string(nb) + " bins";
+        return OPX_ERR_INVALID;
+    }
+    const double *vt = c.cgc_vt[nucleus];
+    double *dev = nullptr;
+    double *part = nullptr;
+    long long *cnt = nullptr;
+    const size_t nout = 1 + (dipole ? (size_t)nb : 0);
+    bool ok = cudaMalloc(&dev, sizeof(double) * nout) == cudaSuccess;
+    const double a1 = c.L.a[1], a2 = c.L.a[2];
+    const double ds = std::min(n1 * a1, n2 * a2) * 0.5 / (double)nb;
+    const int B = 64;
+    const size_t smem = (size_t)nb * B * (sizeof(double) + sizeof(long long));
+    if (dipole && nb > 0) {
+        ok = ok && cudaMalloc(&part, sizeof(double) * ntr * nb) == cudaSuccess;
+        ok = ok && cudaMalloc(&cnt, sizeof(long long) * ntr * nb) == cudaSuccess;
+        if (smem > 200 * 1024) ok = false;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        if (dev) cudaFree(dev);
+        if (part) cudaFree(part);
+        if (cnt) cudaFree(cnt);
+        c.err = "opx_cgc_wilson_lines: out of device memory (or too many dipole bins for shared memory)";
+        return OPX_ERR_NOMEM;
+    }
+    if (c.nc == 2) k_tadpole<2><<<1, 256, 0, c.stream>>>(vt, ntr, dev);
+    else k_tadpole<3><<<1, 256, 0, c.stream>>>(vt, ntr, dev);
+    c.launches++;
+    if (dipole && nb > 0) {
+        if (c.nc == 2) {
+            cudaFuncSetAttribute(k_dipole<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_dipole<2><<<(unsigned)ntr, B, smem, c.stream>>>(vt, n1, n2, a1, a2, nb, ds, part, cnt);
+        } else {
+            cudaFuncSetAttribute(k_dipole<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_dipole<3><<<(unsigned)ntr, B, smem, c.stream>>>(vt, n1, n2, a1, a2, nb, ds, part, cnt);
+        }
+        k_dipole_final<<<grid_for(nb, 128), 128, 0, c.stream>>>(part, cnt, ntr, nb, dev + 1);
+        c.launches += 2;
+    }
+    std::vector<double> host(nout);
+    cudaMemcpyAsync(host.data(), dev, sizeof(double) * nout, cudaMemcpyDeviceToHost, c.stream);
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    cudaFree(dev);
+    if (part) cudaFree(part);
+    if (cnt) cudaFree(cnt);
+    if (e != cudaSuccess) { c.err = std::string("opx_cgc_wilson_lines: ") + cudaGetErrorString(e); return OPX_ERR_CUDA; }
+    if (tadpole) *tadpole = host[0];
+    if (dipole) for (int b = 0; b < nb; b++) dipole[b] = host[1 + b];
+    if (bin_width) *bin_width = ds;
     return OPX_OK;
 }

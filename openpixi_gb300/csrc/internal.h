@@ -99,6 +99,9 @@ struct Ctx {
     double imp_damping = 0.0;
     void *imp_Ua = nullptr, *imp_Ub = nullptr, *imp_E = nullptr;  // the implicit grid's links and E
     std::vector<SuperGroup> sg;  // super-particle groups in list order
+    // Wilson lines at the longitudinal boundary behind each nucleus of the last
+    // opx_cgc_mv / opx_cgc_mv_super call ([n1 n2][ng], reference layout)
+    std::vector<double *> cgc_vt;
     int sg_ppc = 0;
     bool profiling = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -137,6 +140,7 @@ void cpic_free(Ctx &c);
 void launch_cpic_phases(Ctx &c, int reassign);
 void launch_super_phases(Ctx &c, long t);  // CGCSuperParticleInterpolationNGP CIN + JIN at step t
 void super_free(Ctx &c);
+void cgc_vt_free(Ctx &c);  // cgc_kernels.cu
 
 int grid_for(long n, int block);
 

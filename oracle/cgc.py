@@ -25,7 +25,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import OracleGrid, OracleParticles, _p, lib, na, ngen
+from . import OracleGrid, OracleParticles, _p, lib, na, ng, ngen
 
 
 @dataclass
@@ -119,11 +119,13 @@ def mv_nucleus(grid: OracleGrid, nu: MVNucleus, super_particles=False):
         rho[c] = np.where(keep, r, 0.0)
     phi = np.ascontiguousarray(np.stack([poisson2d(rho[c], dims, aT) for c in range(k)]))
     gauss = np.empty((V, na(nc)))
-    L.orc_cgc_solve.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 6
+    vt = np.empty((dims[1] * dims[2], ng(nc)))
+    L.orc_cgc_solve.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 7
     L.orc_cgc_solve(grid.pp, 0, int(nu.orientation), _p(phi), _p(grid.U), _p(grid.Unext), _p(grid.E),
-                    _p(grid.active), _p(gauss))
+                    _p(grid.active), _p(gauss), _p(vt))
+    info = {"rho": rho, "phi": phi, "gauss": gauss, "vt": vt}
     if super_particles:
-        return super_group(grid, gauss, int(nu.orientation)), {"rho": rho, "phi": phi, "gauss": gauss}
+        return super_group(grid, gauss, int(nu.orientation)), info
     L.orc_cgc_particles.restype = C.c_long
     L.orc_cgc_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_long] + [C.c_void_p] * 4
     n = L.orc_cgc_particles(grid.pp, _p(gauss), int(nu.orientation), 0, None, None, None, None)
@@ -133,7 +135,30 @@ def mv_nucleus(grid: OracleGrid, nu: MVNucleus, super_particles=False):
     L.orc_cgc_particles(grid.pp, _p(gauss), int(nu.orientation), n, _p(P.pos0), _p(P.pos1), _p(P.vel), _p(P.Q0))
     P.Q1[...] = P.Q0
     P.dir[...] = 0
-    return P, {"rho": rho, "phi": phi, "gauss": gauss}
+    return P, info
+
+
+def wilson_tadpole(vt, nc):
+    """WilsonLineObservables.computeTadpole (physics/initial/CGC/WilsonLineObservables.java:37-59)."""
+    L = lib()
+    L.orc_wilson_tadpole.restype = C.c_double
+    L.orc_wilson_tadpole.argtypes = [C.c_int, C.c_void_p, C.c_long]
+    v = np.ascontiguousarray(vt, dtype=np.float64)
+    return L.orc_wilson_tadpole(nc, _p(v), v.shape[0])
+
+
+def wilson_dipole(vt, nc, n1, n2, a1=1.0, a2=1.0):
+    """WilsonLineObservables.computeDipole (:67-131): (bin values, bin width)."""
+    L = lib()
+    L.orc_wilson_dipole.restype = C.c_int
+    L.orc_wilson_dipole.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_void_p, C.c_void_p]
+    v = np.ascontiguousarray(vt, dtype=np.float64)
+    nb = L.orc_wilson_dipole(nc, _p(v), n1, n2, a1, a2, None, None)
+    out = np.empty(max(nb, 1))
+    ds = C.c_double()
+    L.orc_wilson_dipole(nc, _p(v), n1, n2, a1, a2, _p(out), C.byref(ds))
+    return out[:nb], ds.value
 
 
 class SuperGroup:

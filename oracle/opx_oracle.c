@@ -1268,7 +1268,7 @@ void orc_mv_charges(const orc_params *p, int direction, double location, double 
  * updated in place (reference layout); gauss: [V][na], the Gauss violation of
  * the nucleus alone (grid copy with its own links, rho of the grid = 0). */
 void orc_cgc_solve(const orc_params *p, int direction, int orientation, const double *phi,
-                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss)
+                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss, double *vt)
 {
     int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
     int ncomp = nc > 1 ? nc * nc - 1 : 1;
@@ -1313,6 +1313,20 @@ void orc_cgc_solve(const orc_params *p, int direction, int orientation, const do
             orc_alg_getlink(nc, a, W);
             orc_group_mult(nc, Vw + (size_t)indexL * ng, W, t2);
             memcpy(Vw + (size_t)index * ng, t2, sizeof(double) * ng);
+        }
+    }
+    /* VT: V at the longitudinal boundary behind the nucleus (:125-136), per transverse cell */
+    if (vt) {
+        int zb = orientation > 0 ? 0 : nL - 1;
+        for (long t = 0; t < ntr; t++) {
+            int pos[3], tp[2], dims_t[2], m = 0;
+            for (int d = 0; d < 3; d++) if (d != direction) dims_t[m++] = p->n[d];
+            tp[0] = (int)(t / dims_t[1]);
+            tp[1] = (int)(t % dims_t[1]);
+            m = 0;
+            for (int d = 0; d < 3; d++) pos[d] = d == direction ? zb : tp[m++];
+            long index = ((long)pos[0] * p->n[1] + pos[1]) * p->n[2] + pos[2];
+            memcpy(vt + (size_t)t * ng, Vw + (size_t)index * ng, sizeof(double) * ng);
         }
     }
     /* links at t = -dt/2 (:143-157) */
@@ -1939,4 +1953,66 @@ int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, co
     }
     free(Ui); free(Uin); free(Ei);
     return 0;
+}
+
+
+/* ---- Wilson-line observables (physics/initial/CGC/WilsonLineObservables.java) ---- */
+
+static double group_retrace(int nc, const double *u)
+{
+    /* GroupElement.getRealTrace: SU(2) 2 e0; SU(3) Re tr */
+    return nc == 2 ? 2.0 * u[0] : u[0] + u[4] + u[8];
+}
+
+/* computeTadpole (:37-59): the mean of Re tr V over the transverse cells, summed in cell order */
+double orc_wilson_tadpole(int nc, const double *vt, long ntr)
+{
+    int ng = orc_ng(nc);
+    double s = 0.0;
+    for (long i = 0; i < ntr; i++) s += group_retrace(nc, vt + (size_t)i * ng);
+    return s / (double)ntr;
+}
+
+/* computeDipole (:67-131): Re tr(V(x) V(y)^dagger) binned by the periodic
+ * transverse distance; nb = (int) sqrt(cells) / 2 bins of width ds =
+ * min(n1 a1, n2 a2) / 2 / nb, i outer and j inner as in the reference.
+ * Returns nb; out (nb values) and ds may be NULL. */
+int orc_wilson_dipole(int nc, const double *vt, int n1, int n2, double a1, double a2, double *out, double *ds_out)
+{
+    int ng = orc_ng(nc);
+    long total = (long)n1 * n2;
+    int nb = (int)sqrt((double)total) / 2;
+    if (!out) return nb;
+    double *sum = calloc((size_t)(nb > 0 ? nb : 1), sizeof(double));
+    long *cnt = calloc((size_t)(nb > 0 ? nb : 1), sizeof(long));
+    double maxd = fmin(n1 * a1, n2 * a2) * 0.5;
+    double ds = maxd / (double)nb;
+    int nn[2] = {n1, n2};
+    double as[2] = {a1, a2};
+    for (long i = 0; i < total; i++) {
+        int x[2] = {(int)(i / n2), (int)(i % n2)};
+        for (long j = 0; j < total; j++) {
+            int y[2] = {(int)(j / n2), (int)(j % n2)};
+            double dist = 0.0;
+            for (int k = 0; k < 2; k++) {
+                double d = fabs((double)(x[k] - y[k]));
+                if (d > nn[k] / 2) d -= nn[k];
+                dist += d * d * as[k] * as[k];
+            }
+            dist = sqrt(dist);
+            int bin = (int)(dist / ds);
+            if (bin < nb) {
+                double adj[NG_MAX], prod[NG_MAX];
+                orc_group_adj(nc, vt + (size_t)j * ng, adj);
+                orc_group_mult(nc, vt + (size_t)i * ng, adj, prod);
+                sum[bin] += group_retrace(nc, prod);
+                cnt[bin]++;
+            }
+        }
+    }
+    for (int b = 0; b < nb; b++) out[b] = sum[b] / (double)cnt[b];
+    if (ds_out) *ds_out = ds;
+    free(sum);
+    free(cnt);
+    return nb;
 }

@@ -149,7 +149,10 @@ void orc_mv_charges(const orc_params *p, int direction, double location, double 
                     int64_t seed, double *out);
 /* LightConePoissonSolverImproved.solve after the Poisson solves */
 void orc_cgc_solve(const orc_params *p, int direction, int orientation, const double *phi,
-                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss);
+                   double *U, double *Unext, double *E, const uint8_t *active, double *gauss, double *vt);
+/* WilsonLineObservables (vt: V at the boundary behind the nucleus, [ntr][ng]) */
+double orc_wilson_tadpole(int nc, const double *vt, long ntr);
+int orc_wilson_dipole(int nc, const double *vt, int n1, int n2, double a1, double a2, double *out, double *ds_out);
 /* LightConeNGPParticleCreator.initializeParticles (beam direction 0) */
 long orc_cgc_particles(const orc_params *p, const double *gauss, int orientation, long cap,
                        double *pos0, double *pos1, double *vel, double *Q);

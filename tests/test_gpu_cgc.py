@@ -125,3 +125,51 @@ def test_cgc_rejects_bad_input(native):
     nu[0]["direction"] = 0
     with pytest.raises(opx.OpixiError):
         hf.cgc_mv(nu)
+
+
+@pytest.mark.parametrize("case", ["su2_two_nuclei", "su3_one_nucleus", "su2_uv_ir_coherence"])
+def test_wilson_line_observables_vs_oracle(native, orc, case):
+    """WilsonLineObservables (tadpole, binned dipole) of every nucleus from the
+    device's Wilson lines against the oracle's (FFT rounding: 1e-10)."""
+    import oracle
+    from oracle import cgc
+    nc, dims, spec = CASES[case]
+    nuclei = [cgc.MVNucleus(**s) for s in spec]
+    g = oracle.OracleGrid(nc, dims, dt=0.5)
+    _, info = cgc.cgc_mv(g, nuclei)
+    h = opx.Handle(nc, dims, dt=0.5)
+    h.cgc_mv(nuclei_args(nuclei))
+    for k, d in enumerate(info):
+        t_ref = cgc.wilson_tadpole(d["vt"], nc)
+        dip_ref, ds_ref = cgc.wilson_dipole(d["vt"], nc, dims[1], dims[2])
+        t, dip, ds = h.cgc_wilson_lines(k)
+        assert abs(t - t_ref) <= 1e-10 * nc, (k, t, t_ref)
+        assert ds == ds_ref
+        assert np.allclose(dip, dip_ref, rtol=0, atol=1e-10 * nc, equal_nan=True), (dip, dip_ref)
+        assert abs(t) < nc  # the nucleus rotates the Wilson lines away from the identity
+    with pytest.raises(opx.OpixiError):
+        h.cgc_wilson_lines(len(info))
+
+
+def test_wilson_line_files(native, tmp_path, monkeypatch):
+    """CGCInitialCondition with computeTadpole / computeDipole writes the
+    reference's files under output/: '<info>, V: <mean>' and the dipole table."""
+    from openpixi_gb300.cgc import CGCInitialCondition, MVModel
+    from openpixi_gb300.settings import Settings
+    from openpixi_gb300.simulation import Simulation
+    monkeypatch.chdir(tmp_path)
+    st = Settings()
+    for i, n in enumerate((24, 8, 8)):
+        st.setGridCells(i, n)
+    st.setGridStep(1.0)
+    st.setTimeStep(0.5)
+    st.setCouplingConstant(1.0)
+    st.setSimulationType("TemporalCGCNGP")
+    ic = CGCInitialCondition(MVModel(0, 1, 12.0, 1.5, 0.5, True, 3))
+    ic.computeTadpole = ic.computeDipole = True
+    st.addInitialConditions(ic)
+    Simulation(st)
+    lines = (tmp_path / "output" / "tadpole.txt").read_text().splitlines()
+    assert len(lines) == 1 and lines[0].startswith("MV, mu: 0.500000, w: 1.500000, UVT: 4.440000") and ", V: " in lines[0]
+    dip = (tmp_path / "output" / "dipole.txt").read_text().splitlines()
+    assert dip[1] == "d\ttr(V V^t)" and len(dip) == 2 + 4

@@ -121,3 +121,74 @@ def test_super_particles_subdivision_invariant_and_gauss(orc, cgc):
     for _ in range(12):
         s2.step()
     assert np.abs(runs[0][0] - g2.U).max() < 1e-3
+
+
+# ---- WilsonLineObservables (physics/initial/CGC/WilsonLineObservables.java) ----
+
+def _dipole_numpy(vt, nc, n1, n2, a1, a2):
+    """Independent restatement of computeDipole (:67-131) with numpy."""
+    total = n1 * n2
+    nb = int(np.sqrt(total)) // 2
+    ds = min(n1 * a1, n2 * a2) * 0.5 / nb
+    pos = np.stack([np.arange(total) // n2, np.arange(total) % n2], 1)
+    d = np.abs(pos[:, None, :] - pos[None, :, :]).astype(float)
+    for k, n in enumerate((n1, n2)):
+        d[..., k] = np.where(d[..., k] > n // 2, d[..., k] - n, d[..., k])
+    dist = np.sqrt(d[..., 0] ** 2 * a1 * a1 + d[..., 1] ** 2 * a2 * a2)
+    b = (dist / ds).astype(int)
+    if nc == 2:
+        tr = 2.0 * vt @ vt.T
+    else:
+        tr = vt @ vt.T  # sum of re*re + im*im over the 9 entries = Re tr(V1 V2^dagger)
+    out = np.array([tr[b == k].mean() if np.any(b == k) else np.nan for k in range(nb)])
+    return out, ds
+
+
+def _random_vt(nc, n, seed):
+    rng = np.random.default_rng(seed)
+    if nc == 2:
+        q = rng.normal(size=(n, 4))
+        return q / np.linalg.norm(q, axis=1, keepdims=True)
+    from scipy.stats import unitary_group
+    out = np.empty((n, 18))
+    for i in range(n):
+        u = unitary_group.rvs(3, random_state=seed * 1000 + i)
+        u = u / np.linalg.det(u) ** (1.0 / 3.0)
+        out[i, :9] = u.real.reshape(-1)
+        out[i, 9:] = u.imag.reshape(-1)
+    return out
+
+
+@pytest.mark.parametrize("nc,n1,n2,a1,a2", [(2, 8, 6, 1.0, 1.0), (2, 7, 9, 0.8, 1.3), (3, 6, 6, 1.0, 1.0)])
+def test_wilson_dipole_matches_numpy(orc, nc, n1, n2, a1, a2):
+    from oracle import cgc
+    vt = _random_vt(nc, n1 * n2, 3)
+    got, ds = cgc.wilson_dipole(vt, nc, n1, n2, a1, a2)
+    ref, ds_ref = _dipole_numpy(vt, nc, n1, n2, a1, a2)
+    assert ds == ds_ref
+    assert np.allclose(got, ref, rtol=1e-13, atol=1e-13, equal_nan=True)
+
+
+def test_wilson_observables_known_answers(orc):
+    """Identity Wilson lines: tadpole N_c, every occupied dipole bin N_c; a
+    global rotation V -> g V leaves the dipole unchanged."""
+    from oracle import cgc
+    for nc, ng in ((2, 4), (3, 18)):
+        vt = np.zeros((64, ng))
+        vt[:, 0] = 1.0
+        if nc == 3:
+            vt[:, 4] = vt[:, 8] = 1.0
+        assert cgc.wilson_tadpole(vt, nc) == float(nc)
+        d, _ = cgc.wilson_dipole(vt, nc, 8, 8)
+        assert np.all(d[np.isfinite(d)] == float(nc))
+    vt = _random_vt(2, 48, 9)
+    g = _random_vt(2, 1, 10)[0]
+    # quaternion product g * V (SU2GroupElement.mult)
+    def qmul(x, a):
+        return np.stack([x[0] * a[:, 0] - x[1] * a[:, 1] - x[2] * a[:, 2] - x[3] * a[:, 3],
+                         x[0] * a[:, 1] + x[1] * a[:, 0] - x[2] * a[:, 3] + x[3] * a[:, 2],
+                         x[0] * a[:, 2] + x[2] * a[:, 0] - x[3] * a[:, 1] + x[1] * a[:, 3],
+                         x[0] * a[:, 3] + x[3] * a[:, 0] - x[1] * a[:, 2] + x[2] * a[:, 1]], 1)
+    d0, _ = cgc.wilson_dipole(vt, 2, 8, 6)
+    d1, _ = cgc.wilson_dipole(qmul(g, vt), 2, 8, 6)
+    assert np.allclose(d0, d1, rtol=1e-13, atol=1e-13, equal_nan=True)
