@@ -224,9 +224,32 @@ int opx_cgc_wilson_lines(opx_ctx *ctx, int nucleus, double *tadpole, double *dip
  * A = log U falls below accuracy_goal; the reference uses 100 and 1e-18),
  * then the occupation numbers n [V][3] (momentum index in cell order, colour
  * inner) and the energy density from them.  n_out may be NULL.  SU(2), one
- * lattice spacing; the optional mirrored grid and cone windows are not provided. */
+ * lattice spacing.  opx_occupation_numbers_ex adds the mirrored grid and the
+ * cone windows. */
 int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accuracy_goal, double *n_out, size_t count,
                            double *energy_density, int *iterations, double *last_divergence);
+
+/* The diagnostic's options (OccupationNumbersInTime.java:92-115, applied in
+ * calculate :164-201): the Coulomb gauge fixed on the grid mirrored along
+ * mirrored_direction (MirroredGrid :655-686; -1 for none) and cut back
+ * (UnmirroredGrid :688-703), then the windows in the order Gaussian
+ * (:555-599), Tukey (:601-653), cone (:506-553), each when its flag is set.
+ * The cone of axis d (cone_velocity[d] != 0) at the grid's time t = steps x dt
+ * spans -/+ |t - collision_time| cone_velocity[d] + collision_position[d]. */
+#define OPX_WINDOW_GAUSSIAN 1
+#define OPX_WINDOW_TUKEY 2
+#define OPX_WINDOW_CONE 4
+typedef struct {
+    int mirrored_direction;
+    int windows;
+    double collision_time;
+    double collision_position[3];
+    double cone_velocity[3];
+    double tukey_width;
+} opx_occupation_options;
+int opx_occupation_numbers_ex(opx_ctx *ctx, const opx_occupation_options *options, int max_iter,
+                              double accuracy_goal, double *n_out, size_t count, double *energy_density,
+                              int *iterations, double *last_divergence);
 
 /* ---- super particles: simulationType "temporal optimized cgc ngp"
  *      (Settings.java:566-571: CGCSuperParticleSolver + CGCSuperParticleInterpolationNGP;

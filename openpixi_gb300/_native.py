@@ -45,7 +45,7 @@ EXPORTED = [
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
     "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
     "opx_super_download", "opx_super_upload", "opx_occupation_numbers", "opx_set_field_solver",
-    "opx_cgc_wilson_lines",
+    "opx_cgc_wilson_lines", "opx_occupation_numbers_ex",
 ]
 
 
@@ -152,6 +152,7 @@ def load(path=None):
         "opx_super_download": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, C.c_size_t]),
         "opx_super_upload": (C.c_int, [vp, C.c_int, C.c_long, C.c_long, vp]),
         "opx_occupation_numbers": (C.c_int, [vp, C.c_int, C.c_double, vp, C.c_size_t, vp, vp, vp]),
+        "opx_occupation_numbers_ex": (C.c_int, [vp, vp, C.c_int, C.c_double, vp, C.c_size_t, vp, vp, vp]),
         "opx_set_field_solver": (C.c_int, [vp, C.c_int, C.c_int, C.c_double]),
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
@@ -172,6 +173,16 @@ def ptr(a):
         return None
     assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"], "C-contiguous numpy array required"
     return a.ctypes.data_as(C.c_void_p)
+
+
+WINDOW_GAUSSIAN, WINDOW_TUKEY, WINDOW_CONE = 1, 2, 4
+
+
+class OccupationOptions(C.Structure):
+    """opx_occupation_options (include/opixi.h)."""
+    _fields_ = [("mirrored_direction", C.c_int), ("windows", C.c_int), ("collision_time", C.c_double),
+                ("collision_position", C.c_double * 3), ("cone_velocity", C.c_double * 3),
+                ("tukey_width", C.c_double)]
 
 
 class Handle:
@@ -356,12 +367,20 @@ class Handle:
         """FastTYMSolver (SOLVER_FAST) or ImplicitTYMSolver(iterations, damping) (SOLVER_IMPLICIT)."""
         self.check(self.L.opx_set_field_solver(self.h, int(kind), int(iterations), float(damping)))
 
-    def occupation_numbers(self, max_iter=100, accuracy_goal=1e-18, with_n=True):
-        """OccupationNumbersInTime: (n [V][3] or None, energy density, iterations, last divergence)."""
+    def occupation_numbers(self, max_iter=100, accuracy_goal=1e-18, with_n=True, mirrored_direction=-1,
+                           windows=0, collision_time=0.0, collision_position=(0.0, 0.0, 0.0),
+                           cone_velocity=(0.0, 0.0, 0.0), tukey_width=0.0):
+        """OccupationNumbersInTime: (n [V][3] or None, energy density, iterations,
+        last divergence); the mirrored grid and the windows (WINDOW_* flags) as
+        the diagnostic's options."""
         n = np.empty((self.V, 3)) if with_n else None
         e, it, dv = C.c_double(), C.c_int(), C.c_double()
-        self.check(self.L.opx_occupation_numbers(self.h, int(max_iter), float(accuracy_goal), ptr(n),
-                                                 0 if n is None else n.size, C.byref(e), C.byref(it), C.byref(dv)))
+        opt = OccupationOptions(int(mirrored_direction), int(windows), float(collision_time),
+                                (C.c_double * 3)(*collision_position), (C.c_double * 3)(*cone_velocity),
+                                float(tukey_width))
+        self.check(self.L.opx_occupation_numbers_ex(self.h, C.byref(opt), int(max_iter), float(accuracy_goal),
+                                                    ptr(n), 0 if n is None else n.size, C.byref(e), C.byref(it),
+                                                    C.byref(dv)))
         return n, e.value, it.value, dv.value
 
     # ---- super particles (temporal optimized cgc ngp) ----

@@ -12,8 +12,12 @@
 //     Fourier transforms of E and of A averaged over U and Unext (18 fields in
 //     one batched transform), occupation numbers per momentum and colour with
 //     the abelian lattice dispersion, and the energy density from them.
-// The optional mirrored grid and cone windows of the diagnostic are not built.
+//   the diagnostic's options (:92-115, :164-201): the mirrored grid (MirroredGrid,
+//     :655-686) on which the Coulomb gauge is fixed before the grid is cut back
+//     (UnmirroredGrid, :688-703), and the Gaussian, Tukey and cone windows
+//     (:555-653, :506-553) applied after the gauge fixing, in that order.
 // Work is in FP64 whatever the handle's precision.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -64,6 +68,132 @@ __global__ void k_occ_copy(const R *__restrict__ U, const R *__restrict__ Un, co
         Uo.store(d, s, Q2<double>{{(double)a.e[0], (double)a.e[1], (double)a.e[2], (double)a.e[3]}});
         Uno.store(d, s, Q2<double>{{(double)b.e[0], (double)b.e[1], (double)b.e[2], (double)b.e[3]}});
         for (int a2 = 0; a2 < 3; a2++) Ec[((long)d * 3 + a2) * L.V + s] = (double)E[((long)d * 3 + a2) * L.V + s];
+    }
+}
+
+// MirroredGrid (:655-686): the grid doubled along md, every cell copied to its
+// own position and to the mirrored one (2 N - 1 - x), and the mirrored copy's
+// link along md taken from the cell one step back (x - 1, or x itself at x = 0)
+template <typename R>
+__global__ void k_occ_copy_mirror(const R *__restrict__ U, const R *__restrict__ Un, const R *__restrict__ E, Lat L,
+                                  Lat Lm, int md, double *__restrict__ Uc, double *__restrict__ Unc,
+                                  double *__restrict__ Ec) {
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    int x[3];
+    site_coords(L, s, x);
+    int y[3] = {x[0], x[1], x[2]};
+    y[md] = 2 * L.n[md] - x[md] - 1;
+    const long s1 = ((long)x[0] * Lm.n[1] + x[1]) * Lm.n[2] + x[2];
+    const long s2 = ((long)y[0] * Lm.n[1] + y[1]) * Lm.n[2] + y[2];
+    int z[3] = {x[0], x[1], x[2]};
+    if (z[md] > 0) z[md]--;
+    const long sh = ((long)z[0] * L.n[1] + z[1]) * L.n[2] + z[2];
+    const LinkPlanes<SU2<R>, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Un), L.V};
+    const LinkPlanes<SU2<double>, double> Uo{Uc, Lm.V}, Uno{Unc, Lm.V};
+    auto wide = [](const Q2<R> &a) { return Q2<double>{{(double)a.e[0], (double)a.e[1], (double)a.e[2], (double)a.e[3]}}; };
+    for (int d = 0; d < 3; d++) {
+        const Q2<double> a = wide(Up.load(d, s)), b = wide(Unp.load(d, s));
+        Uo.store(d, s1, a);
+        Uo.store(d, s2, d == md ? wide(Up.load(d, sh)) : a);
+        Uno.store(d, s1, b);
+        Uno.store(d, s2, b);
+        for (int c = 0; c < 3; c++) {
+            const double e = (double)E[((long)d * 3 + c) * L.V + s];
+            Ec[((long)d * 3 + c) * Lm.V + s1] = e;
+            Ec[((long)d * 3 + c) * Lm.V + s2] = e;
+        }
+    }
+}
+
+// UnmirroredGrid (:688-703): the cells of the first half, at their own positions
+__global__ void k_occ_unmirror(const double *__restrict__ Ucm, const double *__restrict__ Uncm,
+                               const double *__restrict__ Ecm, Lat Lm, Lat L, double *__restrict__ Uc,
+                               double *__restrict__ Unc, double *__restrict__ Ec) {
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    int x[3];
+    site_coords(L, s, x);
+    const long sm = ((long)x[0] * Lm.n[1] + x[1]) * Lm.n[2] + x[2];
+    const LinkPlanes<SU2<double>, double> Ui{const_cast<double *>(Ucm), Lm.V}, Uni{const_cast<double *>(Uncm), Lm.V};
+    const LinkPlanes<SU2<double>, double> Uo{Uc, L.V}, Uno{Unc, L.V};
+    for (int d = 0; d < 3; d++) {
+        Uo.store(d, s, Ui.load(d, sm));
+        Uno.store(d, s, Uni.load(d, sm));
+        for (int c = 0; c < 3; c++) Ec[((long)d * 3 + c) * L.V + s] = Ecm[((long)d * 3 + c) * Lm.V + sm];
+    }
+}
+
+// SU2GroupElement.pow(x) = getLink(x getAlgebraElement()) (math/SU2GroupElement.java:269-271)
+__device__ __forceinline__ Q2<double> su2_pow_ref(const Q2<double> &u, double f) {
+    double v[3];
+    su2_log(u.e, v);
+    for (int c = 0; c < 3; c++) v[c] *= f;
+    Q2<double> r;
+    su2_link_ref(v, r.e);
+    return r;
+}
+
+struct OccWindow {
+    int flags;            // OPX_WINDOW_GAUSSIAN | OPX_WINDOW_TUKEY | OPX_WINDOW_CONE
+    double time, ctime;   // the grid's time (steps x dt) and the collision time
+    double tukey;         // Tukey width
+    double pos[3], vel[3];  // collision position, cone velocity (0: no restriction on the axis)
+};
+
+// GaussianConeRestrictedGrid (:555-599), TukeyConeRestrictedGrid (:601-653) and
+// ConeRestrictedGrid (:506-553), in the order calculate applies them (:194-202).
+// On every axis with a cone velocity the cone spans [minPos, maxPos] with
+// minPos/maxPos = -/+ |t - t_c| v + x_c.  The windows scale E and take U and
+// Unext to the power of their suppression factor; the cone replaces the cells
+// outside it by fresh cells (identity links, E = 0).
+__global__ void k_occ_window(double *__restrict__ U, double *__restrict__ Un, double *__restrict__ E, Lat L,
+                             OccWindow w) {
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    int x[3];
+    site_coords(L, s, x);
+    const double two_sqrt_log_two = 2 * sqrt(log(2.0));
+    const double pi = 3.141592653589793;
+    const LinkPlanes<SU2<double>, double> Up{U, L.V}, Unp{Un, L.V};
+    for (int pass = 0; pass < 3; pass++) {
+        const int flag = pass == 0 ? OPX_WINDOW_GAUSSIAN : (pass == 1 ? OPX_WINDOW_TUKEY : OPX_WINDOW_CONE);
+        if (!(w.flags & flag)) continue;
+        double factor = 1.0;
+        bool inside = true;
+        for (int d = 0; d < 3; d++) {
+            if (w.vel[d] == 0) continue;
+            const double pos = x[d] * L.a[d];
+            const double minTime = -fabs(w.time - w.ctime), maxTime = fabs(w.time - w.ctime);
+            const double minPos = minTime * w.vel[d] + w.pos[d], maxPos = maxTime * w.vel[d] + w.pos[d];
+            if (flag == OPX_WINDOW_GAUSSIAN) {
+                const double sigma = (maxPos - minPos) / two_sqrt_log_two;
+                const double z = (pos - w.pos[d]) / sigma;
+                factor *= exp(-(z * z));
+            } else if (flag == OPX_WINDOW_TUKEY) {
+                const double xx = (pos - w.pos[d]) / (maxPos - minPos), tw = w.tukey;
+                double sup;
+                if ((xx > -.5 - .5 * tw) && (xx <= -.5 + .5 * tw)) sup = 0.5 * (1 + sin(pi * (xx + 0.5) / tw));
+                else if ((xx > -.5 + .5 * tw) && (xx <= .5 - 0.5 * tw)) sup = 1;
+                else if ((xx > 0.5 - 0.5 * tw) && (xx < 0.5 + 0.5 * tw)) sup = 0.5 * (1 - sin(pi * (xx - 0.5) / tw));
+                else sup = 0;
+                factor *= sup;
+            } else if ((pos < minPos) || (pos > maxPos)) {
+                inside = false;
+            }
+        }
+        for (int d = 0; d < 3; d++) {
+            if (flag == OPX_WINDOW_CONE) {
+                if (inside) continue;
+                Up.store(d, s, Q2<double>{{1.0, 0.0, 0.0, 0.0}});
+                Unp.store(d, s, Q2<double>{{1.0, 0.0, 0.0, 0.0}});
+                for (int c = 0; c < 3; c++) E[((long)d * 3 + c) * L.V + s] = 0.0;
+            } else {
+                for (int c = 0; c < 3; c++) E[((long)d * 3 + c) * L.V + s] *= factor;
+                Up.store(d, s, su2_pow_ref(Up.load(d, s), factor));
+                Unp.store(d, s, su2_pow_ref(Unp.load(d, s), factor));
+            }
+        }
     }
 }
 
@@ -210,10 +340,17 @@ __global__ void __launch_bounds__(256) k_occupation(const cufftDoubleComplex *__
 
 using namespace opx;
 
-extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accuracy_goal, double *n_out, size_t count,
-                                      double *energy_density, int *iterations, double *last_divergence) {
+extern "C" int opx_occupation_numbers_ex(opx_ctx *ctx, const opx_occupation_options *opt, int max_iter,
+                                         double accuracy_goal, double *n_out, size_t count, double *energy_density,
+                                         int *iterations, double *last_divergence) {
     if (!ctx) return OPX_ERR_INVALID;
     Ctx &c = ctx_of(ctx);
+    const int md = opt ? opt->mirrored_direction : -1;
+    const int wflags = opt ? opt->windows : 0;
+    if (md < -1 || md > 2 || (wflags & ~(OPX_WINDOW_GAUSSIAN | OPX_WINDOW_TUKEY | OPX_WINDOW_CONE))) {
+        c.err = "opx_occupation_numbers_ex: mirrored_direction -1..2, windows a combination of OPX_WINDOW_*";
+        return OPX_ERR_INVALID;
+    }
     if (c.nc != 2) {
         c.err = "opx_occupation_numbers: SU(2) only (the SU(3) gauge-field logarithm is not provided)";
         return OPX_ERR_UNSUPPORTED;
@@ -226,19 +363,28 @@ extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accurac
         return OPX_ERR_UNSUPPORTED;
     }
     if (!fft_lib().load(c.err)) return OPX_ERR_UNSUPPORTED;
-    const size_t nU = (size_t)link_elems(V, 4);
+    // the lattice the Coulomb gauge is fixed on: the handle's, or the mirrored one
+    int dm[3] = {c.L.n[0], c.L.n[1], c.L.n[2]};
+    if (md >= 0) dm[md] *= 2;
+    const Lat Lm = make_lat(dm, c.L.a, c.L.dt, c.L.g);
+    const long Vm = Lm.V;
+    const size_t nU = (size_t)link_elems(V, 4), nUm = (size_t)link_elems(Vm, 4);
     double *Uc = nullptr, *Unc = nullptr, *Ec = nullptr, *part = nullptr, *nd = nullptr;
+    double *Ucm = nullptr, *Uncm = nullptr, *Ecm = nullptr;
     cufftDoubleComplex *F = nullptr;
-    const int B = 256, nb = (int)std::min<long>(grid_for(V, B), 4L * 152);
+    const int B = 256, nb = (int)std::min<long>(grid_for(Vm, B), 4L * 152);
     bool ok = cudaMalloc(&Uc, sizeof(double) * nU) == cudaSuccess && cudaMalloc(&Unc, sizeof(double) * nU) == cudaSuccess &&
               cudaMalloc(&Ec, sizeof(double) * 9 * V) == cudaSuccess &&
-              cudaMalloc(&F, sizeof(cufftDoubleComplex) * 18 * V) == cudaSuccess &&
+              cudaMalloc(&F, sizeof(cufftDoubleComplex) * std::max(18 * V, 3 * Vm)) == cudaSuccess &&
               cudaMalloc(&part, sizeof(double) * 6 * nb) == cudaSuccess &&
               (!n_out || cudaMalloc(&nd, sizeof(double) * 3 * V) == cudaSuccess);
+    if (md >= 0)
+        ok = ok && cudaMalloc(&Ucm, sizeof(double) * nUm) == cudaSuccess &&
+             cudaMalloc(&Uncm, sizeof(double) * nUm) == cudaSuccess && cudaMalloc(&Ecm, sizeof(double) * 9 * Vm) == cudaSuccess;
     int rc = OPX_OK;
     FFTPlan p3, p18;
     int dims[3] = {c.L.n[0], c.L.n[1], c.L.n[2]};
-    if (ok) ok = p3.make(3, dims, 3, c.stream) && p18.make(3, dims, 18, c.stream);
+    if (ok) ok = p3.make(3, dm, 3, c.stream) && p18.make(3, dims, 18, c.stream);
     if (!ok) {
         cudaGetLastError();
         c.err = "opx_occupation_numbers: out of device memory or cuFFT plan failure";
@@ -247,22 +393,32 @@ extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accurac
     std::vector<double> hp(6 * nb);
     int it = 0;
     double s = 0.0;
+    // the buffers the gauge is fixed in
+    double *Ug = md >= 0 ? Ucm : Uc, *Ung = md >= 0 ? Uncm : Unc, *Eg = md >= 0 ? Ecm : Ec;
     if (!rc) {
-        if (c.prec == OPX_F64)
+        if (md >= 0) {
+            if (c.prec == OPX_F64)
+                k_occ_copy_mirror<double><<<grid_for(V, B), B, 0, c.stream>>>(
+                    (const double *)c.U, (const double *)c.Unext, (const double *)c.E, c.L, Lm, md, Ug, Ung, Eg);
+            else
+                k_occ_copy_mirror<float><<<grid_for(V, B), B, 0, c.stream>>>(
+                    (const float *)c.U, (const float *)c.Unext, (const float *)c.E, c.L, Lm, md, Ug, Ung, Eg);
+        } else if (c.prec == OPX_F64) {
             k_occ_copy<double><<<grid_for(V, B), B, 0, c.stream>>>((const double *)c.U, (const double *)c.Unext,
                                                                    (const double *)c.E, c.L, Uc, Unc, Ec);
-        else
+        } else {
             k_occ_copy<float><<<grid_for(V, B), B, 0, c.stream>>>((const float *)c.U, (const float *)c.Unext,
                                                                   (const float *)c.E, c.L, Uc, Unc, Ec);
+        }
         c.launches++;
         // CoulombGauge.applyGaugeTransformation (:56-75)
         while (it < max_iter && !rc) {
-            k_coulomb_div<<<nb, B, 0, c.stream>>>(Uc, c.L, F, part);
+            k_coulomb_div<<<nb, B, 0, c.stream>>>(Ug, Lm, F, part);
             cudaMemcpyAsync(hp.data(), part, sizeof(double) * 6 * nb, cudaMemcpyDeviceToHost, c.stream);
             if (fft_lib().execZ2Z(p3.h, F, F, CUFFT_FORWARD) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
-            k_inverse_laplace<<<grid_for(V, B), B, 0, c.stream>>>(F, c.L);
+            k_inverse_laplace<<<grid_for(Vm, B), B, 0, c.stream>>>(F, Lm);
             if (fft_lib().execZ2Z(p3.h, F, F, CUFFT_INVERSE) != CUFFT_SUCCESS) rc = OPX_ERR_CUDA;
-            k_coulomb_apply<<<grid_for(V, B), B, 0, c.stream>>>(F, c.L, Uc, Unc, Ec);
+            k_coulomb_apply<<<grid_for(Vm, B), B, 0, c.stream>>>(F, Lm, Ug, Ung, Eg);
             c.launches += 5;
             cudaError_t e = cudaStreamSynchronize(c.stream);
             if (e != cudaSuccess) { c.err = std::string("opx_occupation_numbers: ") + cudaGetErrorString(e); rc = OPX_ERR_CUDA; break; }
@@ -277,6 +433,20 @@ extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accurac
             if (s < accuracy_goal) break;
         }
         if (rc && c.err.empty()) c.err = "opx_occupation_numbers: cuFFT execution failed";
+    }
+    if (!rc && md >= 0) {
+        k_occ_unmirror<<<grid_for(V, B), B, 0, c.stream>>>(Ucm, Uncm, Ecm, Lm, c.L, Uc, Unc, Ec);
+        c.launches++;
+    }
+    if (!rc && wflags) {
+        OccWindow w;
+        w.flags = wflags;
+        w.time = (double)c.steps * c.L.dt;  // grid.getSimulationSteps() * grid.getTemporalSpacing()
+        w.ctime = opt->collision_time;
+        w.tukey = opt->tukey_width;
+        for (int d = 0; d < 3; d++) { w.pos[d] = opt->collision_position[d]; w.vel[d] = opt->cone_velocity[d]; }
+        k_occ_window<<<grid_for(V, B), B, 0, c.stream>>>(Uc, Unc, Ec, c.L, w);
+        c.launches++;
     }
     double energy = 0.0;
     if (!rc) {
@@ -301,11 +471,17 @@ extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accurac
             energy = (v.s + v.c) * (1.0 / (2.0 * box * box));
         }
     }
-    void *bufs[] = {Uc, Unc, Ec, F, part, nd};
+    void *bufs[] = {Uc, Unc, Ec, F, part, nd, Ucm, Uncm, Ecm};
     for (void *b : bufs) if (b) cudaFree(b);
     if (rc) return rc;
     if (energy_density) *energy_density = energy;
     if (iterations) *iterations = it;
     if (last_divergence) *last_divergence = s;
     return OPX_OK;
+}
+
+extern "C" int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accuracy_goal, double *n_out, size_t count,
+                                      double *energy_density, int *iterations, double *last_divergence) {
+    return opx_occupation_numbers_ex(ctx, nullptr, max_iter, accuracy_goal, n_out, count, energy_density, iterations,
+                                     last_divergence);
 }

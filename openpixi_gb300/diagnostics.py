@@ -169,17 +169,30 @@ class OccupationNumbersInTime(Diagnostics):
     (+ the momentum vectors for "csv_with_vectors"), then per measurement
     "time, energy" and the occupation numbers (one line per colour when
     colorful, else their colour sum); "csv_only_energy" writes the first line
-    only, "none" nothing.  The mirrored grid and cone windows are not provided."""
+    only, "none" nothing.  The options of the long constructor (:99-115): the
+    Coulomb gauge on the grid mirrored along mirroredDirection, and the
+    Gaussian, Tukey and rectangular (cone) windows."""
 
     TYPES = ("csv", "csv_only_energy", "csv_with_vectors", "none")
 
-    def __init__(self, interval, output_type, path, colorful=False, max_iter=100, accuracy_goal=1e-18):
+    def __init__(self, interval, output_type, path, colorful=False, max_iter=100, accuracy_goal=1e-18,
+                 useMirroredGrid=False, mirroredDirection=0, useCone=False, collisionTime=0.0,
+                 collisionPosition=(0.0, 0.0, 0.0), coneVelocity=(0.0, 0.0, 0.0), useGaussianWindow=False,
+                 useTukeyWindow=False, tukeyWidth=0.0):
         self.timeInterval = float(interval)
         self.outputType = output_type
         self.path = path
         self.colorful = bool(colorful)
         self.maxIter = int(max_iter)
         self.accuracyGoal = float(accuracy_goal)
+        from ._native import WINDOW_CONE, WINDOW_GAUSSIAN, WINDOW_TUKEY
+        self.mirroredDirection = int(mirroredDirection) if useMirroredGrid else -1
+        self.windows = ((WINDOW_GAUSSIAN if useGaussianWindow else 0) | (WINDOW_TUKEY if useTukeyWindow else 0)
+                        | (WINDOW_CONE if useCone else 0))
+        self.collisionTime = float(collisionTime)
+        self.collisionPosition = tuple(float(v) for v in collisionPosition)
+        self.coneVelocity = tuple(float(v) for v in coneVelocity)
+        self.tukeyWidth = float(tukeyWidth)
         self.computationCounter = 0
         self.occupationNumbers = None
         self.energyDensity = None
@@ -211,7 +224,12 @@ class OccupationNumbersInTime(Diagnostics):
         if steps % self.stepInterval != 0:
             return
         n, e, it, dv = grid.handle.occupation_numbers(self.maxIter, self.accuracyGoal,
-                                                      with_n=self.outputType != "csv_only_energy")
+                                                      with_n=self.outputType != "csv_only_energy",
+                                                      mirrored_direction=self.mirroredDirection,
+                                                      windows=self.windows, collision_time=self.collisionTime,
+                                                      collision_position=self.collisionPosition,
+                                                      cone_velocity=self.coneVelocity,
+                                                      tukey_width=self.tukeyWidth)
         self.occupationNumbers, self.energyDensity = n, e
         if self.outputType != "none":
             with open(self.path, "a") as f:
@@ -259,9 +277,18 @@ def from_yaml(out):
     for o in out.get("timeMeasurement") or []:
         ds.append(TimeMeasurement(o["path"], o["interval"]))
     for o in out.get("occupationNumbersInTime") or []:
+        kw = {}
         if o.get("useMirroredGrid") is not None:
-            raise NotImplementedError("OccupationNumbersInTime: the mirrored grid and cone windows are not provided")
-        ds.append(OccupationNumbersInTime(o["interval"], o["outputType"], o["path"], bool(o.get("colorful", False))))
+            # YamlOccupationNumbersInTime.getFileGenerator: the long constructor
+            kw = dict(useMirroredGrid=bool(o["useMirroredGrid"]), mirroredDirection=o.get("mirroredDirection", 0),
+                      useCone=bool(o.get("useRectangularWindow", False)),
+                      collisionTime=o.get("collisionTime", 0.0),
+                      collisionPosition=o.get("collisionPosition", [0.0, 0.0, 0.0]),
+                      coneVelocity=o.get("coneVelocity", [0.0, 0.0, 0.0]),
+                      useGaussianWindow=bool(o.get("useGaussianWindow", False)),
+                      useTukeyWindow=bool(o.get("useTukeyWindow", False)), tukeyWidth=o.get("tukeyWidth", 0.0))
+        ds.append(OccupationNumbersInTime(o["interval"], o["outputType"], o["path"], bool(o.get("colorful", False)),
+                                          **kw))
     unsupported = set(out) - {"bulkQuantitiesInTime", "energyDensity", "projectedEnergyDensity", "timeMeasurement",
                               "occupationNumbersInTime"}
     if unsupported:

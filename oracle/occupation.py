@@ -61,11 +61,122 @@ def coulomb_gauge(grid: OracleGrid, max_iter=100, goal=1e-18):
     return conv
 
 
-def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18):
+def mirrored_grid(grid: OracleGrid, md):
+    """MirroredGrid (OccupationNumbersInTime.java:655-686): dims[md] doubled; each
+    cell copied to x and to 2N - 1 - x along md, the mirrored copy's link along
+    md taken from the cell at x - 1 (x itself at x = 0)."""
+    dims = list(grid.dims)
+    n = dims[md]
+    dims[md] *= 2
+    m = OracleGrid(grid.nc, dims, grid.a, grid.dt, grid.g)
+    x = np.indices(grid.dims).reshape(3, -1)
+    def idx(pos, dd):
+        return (pos[0] * dd[1] + pos[1]) * dd[2] + pos[2]
+    i1 = idx(x, dims)
+    y = x.copy()
+    y[md] = 2 * n - x[md] - 1
+    i2 = idx(y, dims)
+    z = x.copy()
+    z[md] = np.where(z[md] > 0, z[md] - 1, z[md])
+    ish = idx(z, grid.dims)
+    for k in ("U", "Unext", "E"):
+        getattr(m, k)[i1] = getattr(grid, k)
+        getattr(m, k)[i2] = getattr(grid, k)
+    m.U[i2, md] = grid.U[ish, md]
+    return m
+
+
+def unmirrored_grid(m: OracleGrid, md, dims):
+    """UnmirroredGrid (:688-703): the cells of the first half at their own positions."""
+    g = OracleGrid(m.nc, dims, m.a, m.dt, m.g)
+    x = np.indices(dims).reshape(3, -1)
+    im = (x[0] * m.dims[1] + x[1]) * m.dims[2] + x[2]
+    for k in ("U", "Unext", "E"):
+        getattr(g, k)[...] = getattr(m, k)[im]
+    return g
+
+
+def _su2_pow(u, f):
+    """SU2GroupElement.pow(x) = getLink(x getAlgebraElement()) (math/SU2GroupElement.java:234-271,
+    math/SU2AlgebraElement.java:140-152), vectorised over the last-but-one axes."""
+    norm = np.sqrt(u[..., 1] ** 2 + u[..., 2] ** 2 + u[..., 3] ** 2)
+    small = norm < 1e-15
+    with np.errstate(invalid="ignore"):
+        fac = np.where(small, 2.0, 2.0 * np.arcsin(norm) / np.where(small, 1.0, norm))
+    v = u[..., 1:] * fac[..., None] * f[..., None]
+    mod = np.sqrt((v ** 2).sum(-1)) / 2
+    sinfakt = np.where(mod < 1e-20, 0.0, 0.5 / np.where(mod < 1e-20, 1.0, mod) * np.sin(mod))
+    out = np.empty_like(u)
+    out[..., 0] = np.cos(mod)
+    out[..., 1:] = v * sinfakt[..., None]
+    return out
+
+
+GAUSSIAN, TUKEY, CONE = 1, 2, 4
+
+
+def windows(g: OracleGrid, flags, time, ctime, cpos, cvel, tukey):
+    """GaussianConeRestrictedGrid (:555-599), TukeyConeRestrictedGrid (:601-653)
+    and ConeRestrictedGrid (:506-553) in the order calculate applies them
+    (:194-202), in place."""
+    x = np.indices(g.dims).reshape(3, -1)
+    two_sqrt_log_two = 2 * np.sqrt(np.log(2))
+    for flag in (GAUSSIAN, TUKEY, CONE):
+        if not flags & flag:
+            continue
+        factor = np.ones(g.V)
+        inside = np.ones(g.V, bool)
+        for d in range(3):
+            if cvel[d] == 0:
+                continue
+            pos = x[d] * g.a[d]
+            min_t, max_t = -abs(time - ctime), abs(time - ctime)
+            min_p, max_p = min_t * cvel[d] + cpos[d], max_t * cvel[d] + cpos[d]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                if flag == GAUSSIAN:
+                    sigma = (max_p - min_p) / two_sqrt_log_two
+                    factor *= np.exp(-(((pos - cpos[d]) / sigma) ** 2))
+                elif flag == TUKEY:
+                    xx = (pos - cpos[d]) / (max_p - min_p)
+                    w = tukey
+                    sup = np.zeros(g.V)
+                    m1 = (xx > -.5 - .5 * w) & (xx <= -.5 + .5 * w)
+                    m2 = (xx > -.5 + .5 * w) & (xx <= .5 - 0.5 * w)
+                    m3 = (xx > 0.5 - 0.5 * w) & (xx < 0.5 + 0.5 * w)
+                    sup = np.where(m1, 0.5 * (1 + np.sin(np.pi * (xx + 0.5) / w)), sup)
+                    sup = np.where(m2 & ~m1, 1.0, sup)
+                    sup = np.where(m3 & ~m1 & ~m2, 0.5 * (1 - np.sin(np.pi * (xx - 0.5) / w)), sup)
+                    factor *= sup
+                else:
+                    inside &= ~((pos < min_p) | (pos > max_p))
+        if flag == CONE:
+            out = ~inside
+            g.U[out] = np.array([1.0, 0.0, 0.0, 0.0])
+            g.Unext[out] = np.array([1.0, 0.0, 0.0, 0.0])
+            g.E[out] = 0.0
+        else:
+            g.E *= factor[:, None, None]
+            f3 = np.repeat(factor[:, None], 3, 1)
+            g.U[...] = _su2_pow(g.U, f3)
+            g.Unext[...] = _su2_pow(g.Unext, f3)
+
+
+def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18, mirrored_direction=-1, window_flags=0,
+                       time=0.0, collision_time=0.0, collision_position=(0.0, 0.0, 0.0),
+                       cone_velocity=(0.0, 0.0, 0.0), tukey_width=0.0):
     """OccupationNumbersInTime.calculate on a copy of the grid: returns
-    (n [V][3], energy density, divergence list).  Isotropic lattice spacing."""
-    g = grid.copy()
-    conv = coulomb_gauge(g, max_iter, goal)
+    (n [V][3], energy density, divergence list).  Isotropic lattice spacing.
+    Options as in the diagnostic's constructor (:92-115); time is the grid's
+    time, steps x dt."""
+    if mirrored_direction >= 0:
+        gm = mirrored_grid(grid, mirrored_direction)
+        conv = coulomb_gauge(gm, max_iter, goal)
+        g = unmirrored_grid(gm, mirrored_direction, grid.dims)
+    else:
+        g = grid.copy()
+        conv = coulomb_gauge(g, max_iter, goal)
+    if window_flags:
+        windows(g, window_flags, time, collision_time, collision_position, cone_velocity, tukey_width)
     V, dims = g.V, g.dims
     a = g.a[0]
     gainv = 1.0 / (a * g.g)

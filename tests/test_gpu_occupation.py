@@ -70,3 +70,42 @@ def test_occupation_rejects_su3(native):
     h = opx.Handle(3, (4, 4, 4))
     with pytest.raises(opx.OpixiError):
         h.occupation_numbers()
+
+
+OPTION_CASES = {
+    "mirrored_0": dict(mirrored_direction=0),
+    "mirrored_2": dict(mirrored_direction=2),
+    "gaussian": dict(window_flags=1, collision_time=0.0, collision_position=(4.0, 3.0, 5.0),
+                     cone_velocity=(1.0, 0.0, 0.0)),
+    "tukey": dict(window_flags=2, collision_time=0.0, collision_position=(4.0, 3.0, 5.0),
+                  cone_velocity=(1.0, 0.0, 0.5), tukey_width=0.4),
+    "cone": dict(window_flags=4, collision_time=0.0, collision_position=(4.0, 3.0, 5.0),
+                 cone_velocity=(1.0, 1.0, 0.0)),
+    "mirrored_all_windows": dict(mirrored_direction=0, window_flags=7, collision_time=0.0,
+                                 collision_position=(4.0, 3.0, 5.0), cone_velocity=(1.0, 0.0, 1.0),
+                                 tukey_width=0.5),
+}
+
+
+@pytest.mark.parametrize("case", sorted(OPTION_CASES))
+def test_occupation_options_vs_oracle(native, orc, case):
+    """The mirrored grid and the Gaussian, Tukey and cone windows
+    (OccupationNumbersInTime.java:92-115, :164-201, :506-703) against the
+    oracle: occupation numbers within 1e-9 of the largest, energy 1e-10."""
+    from oracle import occupation
+    opt = OPTION_CASES[case]
+    g = orc.OracleGrid(2, (8, 6, 10), dt=0.5, g=1.1)
+    g.random_links(7, 0.15)
+    g.random_e(7, 0.1)
+    g.update_links()
+    h = handle_of(g)
+    h.step(6)  # the windows use the grid's time, steps x dt = 3
+    g.U[...] = h.download(N.FIELD_U)
+    g.Unext[...] = h.download(N.FIELD_UNEXT)
+    g.E[...] = h.download(N.FIELD_E)
+    n_ref, e_ref, conv = occupation.occupation_numbers(g, time=6 * 0.5, **opt)
+    kw = {("windows" if k == "window_flags" else k): v for k, v in opt.items()}
+    n, e, it, dv = h.occupation_numbers(**kw)
+    assert it == len(conv)
+    assert np.abs(n - n_ref).max() <= 1e-9 * np.abs(n_ref).max()
+    assert abs(e - e_ref) <= 1e-10 * abs(e_ref)

@@ -79,3 +79,43 @@ def test_occupation_gauge_invariant(orc, occ):
     assert abs(e1 - e0) <= 1e-6 * e0
     s0, s1 = n0.sum(axis=1), n1.sum(axis=1)
     assert np.abs(s1 - s0).max() <= 1e-5 * np.abs(s0).max()
+
+
+def test_mirror_roundtrip_and_windows(orc):
+    """MirroredGrid then UnmirroredGrid gives the grid back exactly; the
+    mirrored copy holds the cells mirrored, with the shifted link along the
+    mirrored direction; the cone window resets the cells outside it; the
+    Tukey window is 1 on its plateau and 0 outside."""
+    from oracle import occupation as oc
+    g = orc.OracleGrid(2, (4, 3, 5), dt=0.5)
+    g.random_links(3, 0.3)
+    g.random_e(3, 0.2)
+    g.update_links()
+    for md in range(3):
+        m = oc.mirrored_grid(g, md)
+        back = oc.unmirrored_grid(m, md, g.dims)
+        for k in ("U", "Unext", "E"):
+            assert np.array_equal(getattr(back, k), getattr(g, k))
+        n = g.dims[md]
+        x = np.indices(g.dims).reshape(3, -1)
+        y = x.copy()
+        y[md] = 2 * n - 1 - x[md]
+        dm = m.dims
+        i2 = (y[0] * dm[1] + y[1]) * dm[2] + y[2]
+        assert np.array_equal(m.E[i2], g.E)
+        z = x.copy()
+        z[md] = np.maximum(z[md] - 1, 0)
+        ish = (z[0] * g.dims[1] + z[1]) * g.dims[2] + z[2]
+        assert np.array_equal(m.U[i2, md], g.U[ish, md])
+    c = g.copy()
+    oc.windows(c, oc.CONE, 1.0, 0.0, (1.0, 0.0, 0.0), (1.0, 0.0, 0.0), 0.0)
+    x0 = np.arange(g.V) // (g.dims[1] * g.dims[2])
+    outside = (x0 < 0) | (x0 > 2)
+    assert np.all(c.U[outside] == np.array([1.0, 0, 0, 0])) and np.all(c.E[outside] == 0)
+    assert np.array_equal(c.E[~outside], g.E[~outside])
+    t = g.copy()
+    # Tukey, width 0.5: plateau for |x| <= 0.25, zero for |x| >= 0.75 (x = (pos - c) / (maxPos - minPos))
+    oc.windows(t, oc.TUKEY, 2.0, 0.0, (2.0, 0.0, 0.0), (1.0, 0.0, 0.0), 0.5)
+    xx = (x0 * 1.0 - 2.0) / 4.0
+    plateau = np.abs(xx) <= 0.25
+    assert np.allclose(t.E[plateau], g.E[plateau], rtol=0, atol=0)
