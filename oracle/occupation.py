@@ -1,4 +1,4 @@
-"""CPU oracle of the Coulomb gauge and the occupation numbers (SU(2)).
+"""CPU oracle of the Coulomb gauge and the occupation numbers (SU(2), SU(3)).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``; the GPU product never
 imports it.
@@ -38,20 +38,19 @@ def _inverse_laplace(dims):
 def coulomb_gauge(grid: OracleGrid, max_iter=100, goal=1e-18):
     """CoulombGauge.applyGaugeTransformation (:56-75) on the grid's U, Unext, E;
     returns the list of divergences (one per iteration)."""
-    if grid.nc != 2:
-        raise ValueError("SU(2) only")
     L = lib()
     L.orc_coulomb_divergence.restype = C.c_double
     L.orc_coulomb_divergence.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.orc_coulomb_apply.argtypes = [C.c_void_p] * 5
     V, dims = grid.V, grid.dims
+    ncomp = 3 if grid.nc == 2 else 8
     inv = _inverse_laplace(dims)
     conv = []
-    div = np.empty((3, V))
+    div = np.empty((ncomp, V))
     while len(conv) < max_iter:
         s = L.orc_coulomb_divergence(grid.pp, _p(grid.U), _p(div))
-        psi = np.empty((3, V))
-        for c in range(3):
+        psi = np.empty((ncomp, V))
+        for c in range(ncomp):
             f = np.fft.fftn(div[c].reshape(dims).astype(complex))
             psi[c] = np.fft.ifftn(f * inv).real.reshape(-1)
         L.orc_coulomb_apply(grid.pp, _p(np.ascontiguousarray(psi)), _p(grid.U), _p(grid.Unext), _p(grid.E))
@@ -176,17 +175,20 @@ def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18, mirrored_dire
         g = grid.copy()
         conv = coulomb_gauge(g, max_iter, goal)
     if window_flags:
+        if g.nc != 2:
+            raise ValueError("the windows take SU(2) powers of the links")
         windows(g, window_flags, time, collision_time, collision_position, cone_velocity, tukey_width)
     V, dims = g.V, g.dims
+    ncomp = 3 if g.nc == 2 else 8
     a = g.a[0]
     gainv = 1.0 / (a * g.g)
-    Ef = np.empty((3, 3, V))
-    A = np.empty((3, 3, V))
+    Ef = np.empty((3, ncomp, V))
+    A = np.empty((3, ncomp, V))
     L = lib()
     L.orc_occupation_fields.argtypes = [C.c_void_p] * 4 + [C.c_double, C.c_void_p, C.c_void_p]
     L.orc_occupation_fields(g.pp, _p(g.U), _p(g.Unext), _p(g.E), gainv, _p(Ef), _p(A))
-    eF = np.fft.fftn(Ef.reshape(3, 3, *dims), axes=(2, 3, 4)).reshape(3, 3, V)
-    aF = np.fft.fftn(A.reshape(3, 3, *dims), axes=(2, 3, 4)).reshape(3, 3, V)
+    eF = np.fft.fftn(Ef.reshape(3, ncomp, *dims), axes=(2, 3, 4)).reshape(3, ncomp, V)
+    aF = np.fft.fftn(A.reshape(3, ncomp, *dims), axes=(2, 3, 4)).reshape(3, ncomp, V)
     deff = sum(1 for d in dims if d > 1)
     conv_f = a ** (2 * deff)
     # lattice momenta and the abelian lattice dispersion (:301-312, :334-355)
@@ -198,8 +200,8 @@ def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18, mirrored_dire
         k = np.where(delta < 0.5, 2.0 * delta * np.pi / a, 2.0 * (delta - 1.0) * np.pi / a)
         w2 += 2.0 * (1.0 - np.cos(k * a)) / (a * a)
     w = np.sqrt(w2)
-    n = np.empty((V, 3))
-    for k in range(3):
+    n = np.empty((V, ncomp))
+    for k in range(ncomp):
         e2 = sum(eF[j, k].real ** 2 + eF[j, k].imag ** 2 for j in range(3))
         a2 = sum(aF[j, k].real ** 2 + aF[j, k].imag ** 2 for j in range(3))
         mixed = -sum(2.0 * (-aF[j, k].imag * eF[j, k].real + aF[j, k].real * eF[j, k].imag) for j in range(3))

@@ -6,6 +6,7 @@
  */
 #include "opx_oracle.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -318,6 +319,230 @@ static void su3_from_gen(const double *gen, double *v)
         }
     }
     memcpy(v, w, sizeof(w));
+}
+
+/* SU3GroupElement.getAlgebraElement (math/SU3GroupElement.java:476-490): the
+ * hermitian H with exp(i H) = U, restated with methods of our own (the
+ * reference solves the characteristic cubic, builds eigenvectors and falls
+ * back to a Taylor series near the identity and for degenerate eigenvalues).
+ *
+ * su3_log: inverse scaling and squaring.  Principal square roots (the
+ * Denman-Beavers iteration) halve U's eigenphases until ||U' - I||_F <= 0.5,
+ * then log U' = 2 atanh(Z), Z = (U' - I)(U' + I)^-1, by its odd power series,
+ * and log U = 2^k log U'.  This is the principal logarithm; when its trace is
+ * not 0 (the eigenphases add up to +-2 pi) the reference instead takes the
+ * phase sum off one eigenvalue, which su3_log_eigen does.
+ *
+ * su3_log_eigen: the eigenvalues are the roots of l^3 - a l^2 + b l - det U
+ * (Cardano in complex arithmetic, two Newton steps), the eigenvector of a
+ * simple eigenvalue the largest column of (U - l_i)(U - l_j); the phase sum is
+ * taken off the first phase.  Accurate for well separated eigenvalues. */
+static void su3_log_eigen(const double *u, double *v)
+{
+    double complex M[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) M[i][j] = u[3 * i + j] + I * u[9 + 3 * i + j];
+    double complex a = M[0][0] + M[1][1] + M[2][2], tr2 = 0;
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) tr2 += M[i][k] * M[k][i];
+    double complex b = (a * a - tr2) / 2;
+    double complex det = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                         M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                         M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    double complex p = b - a * a / 3, q = -2.0 * a * a * a / 27 + a * b / 3 - det;
+    double complex disc = q * q / 4 + p * p * p / 27, sq = csqrt(disc);
+    double complex w3 = -q / 2 + sq;
+    if (cabs(-q / 2 - sq) > cabs(w3)) w3 = -q / 2 - sq;
+    double complex lam[3];
+    if (cabs(w3) < 1e-300) {
+        for (int k = 0; k < 3; k++) lam[k] = a / 3;
+    } else {
+        double complex w = cpow(w3, 1.0 / 3.0), om = cexp(2.0 * M_PI * I / 3.0);
+        for (int k = 0; k < 3; k++) {
+            lam[k] = w - p / (3.0 * w) + a / 3;
+            w *= om;
+        }
+    }
+    for (int k = 0; k < 3; k++)
+        for (int it = 0; it < 2; it++) {
+            double complex l = lam[k];
+            double complex f = ((l - a) * l + b) * l - det, df = (3.0 * l - 2.0 * a) * l + b;
+            if (cabs(df) > 1e-300) lam[k] = l - f / df;
+        }
+    double th[3];
+    for (int k = 0; k < 3; k++) th[k] = carg(lam[k]);
+    th[0] -= th[0] + th[1] + th[2];
+    /* coincident eigenvalues */
+    int same01 = cabs(lam[0] - lam[1]) < 1e-9, same02 = cabs(lam[0] - lam[2]) < 1e-9,
+        same12 = cabs(lam[1] - lam[2]) < 1e-9;
+    double complex H[3][3] = {{0}};
+    if (same01 && same02) {
+        double t = carg((lam[0] + lam[1] + lam[2]) / 3.0);
+        for (int i = 0; i < 3; i++) H[i][i] = t;
+    } else {
+        int simple[3] = {1, 1, 1}, ks = -1, kd0 = -1, kd1 = -1;
+        if (same01) { simple[0] = simple[1] = 0; ks = 2; kd0 = 0; kd1 = 1; }
+        else if (same02) { simple[0] = simple[2] = 0; ks = 1; kd0 = 0; kd1 = 2; }
+        else if (same12) { simple[1] = simple[2] = 0; ks = 0; kd0 = 1; kd1 = 2; }
+        double complex vec[3][3];
+        for (int k = 0; k < 3; k++) {
+            if (!simple[k] && k != ks) continue;
+            int i = (k + 1) % 3, j = (k + 2) % 3;
+            double complex A[3][3], B[3][3], P[3][3];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    A[r][c] = M[r][c] - (r == c ? lam[i] : 0);
+                    B[r][c] = M[r][c] - (r == c ? lam[j] : 0);
+                }
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    P[r][c] = 0;
+                    for (int m = 0; m < 3; m++) P[r][c] += A[r][m] * B[m][c];
+                }
+            int best = 0;
+            double bn = -1;
+            for (int c = 0; c < 3; c++) {
+                double n = 0;
+                for (int r = 0; r < 3; r++) n += creal(P[r][c] * conj(P[r][c]));
+                if (n > bn) { bn = n; best = c; }
+            }
+            double nrm = sqrt(bn);
+            for (int r = 0; r < 3; r++) vec[k][r] = nrm > 0 ? P[r][best] / nrm : (r == k ? 1.0 : 0.0);
+        }
+        if (ks < 0) {
+            for (int k = 0; k < 3; k++)
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) H[r][c] += th[k] * vec[k][r] * conj(vec[k][c]);
+        } else {
+            /* the simple eigenvalue's phase carries the trace correction of th[0] */
+            double ts = th[ks], td = carg((lam[kd0] + lam[kd1]) / 2.0);
+            double sum = ts + 2 * td;
+            ts -= sum;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    double complex pr = vec[ks][r] * conj(vec[ks][c]);
+                    H[r][c] = ts * pr + td * ((r == c ? 1.0 : 0.0) - pr);
+                }
+        }
+    }
+    double vals[18];
+    for (int i = 0; i < 9; i++) { vals[i] = creal(H[i / 3][i % 3]); vals[9 + i] = cimag(H[i / 3][i % 3]); }
+    su3_hermiticize(vals, v);
+}
+
+typedef double complex cm3[3][3];
+
+static void cm3_mul(const cm3 A, const cm3 B, cm3 C)
+{
+    cm3 T;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            double complex t = 0;
+            for (int m = 0; m < 3; m++) t += A[r][m] * B[m][c];
+            T[r][c] = t;
+        }
+    memcpy(C, T, sizeof(cm3));
+}
+
+/* inverse by the adjugate */
+static void cm3_inv(const cm3 A, cm3 B)
+{
+    cm3 T;
+    T[0][0] = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+    T[0][1] = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+    T[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+    T[1][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+    T[1][1] = A[0][0] * A[2][2] - A[0][2] * A[2][0];
+    T[1][2] = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+    T[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    T[2][1] = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+    T[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    double complex det = A[0][0] * T[0][0] + A[0][1] * T[1][0] + A[0][2] * T[2][0];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) B[r][c] = T[r][c] / det;
+}
+
+static double cm3_dist_id(const cm3 A)
+{
+    double n = 0;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            double complex d = A[r][c] - (r == c ? 1.0 : 0.0);
+            n += creal(d * conj(d));
+        }
+    return sqrt(n);
+}
+
+static void su3_log(const double *u, double *v)
+{
+    cm3 Y, Z, Yi, Zi, L;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) Y[i][j] = u[3 * i + j] + I * u[9 + 3 * i + j];
+    int k = 0;
+    while (cm3_dist_id(Y) > 0.5 && k < 30) {
+        /* Denman-Beavers: Y -> sqrt(Y) */
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) Z[r][c] = r == c ? 1.0 : 0.0;
+        for (int it = 0; it < 50; it++) {
+            cm3_inv(Y, Yi);
+            cm3_inv(Z, Zi);
+            double change = 0;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    double complex yn = 0.5 * (Y[r][c] + Zi[r][c]);
+                    Z[r][c] = 0.5 * (Z[r][c] + Yi[r][c]);
+                    change += cabs(yn - Y[r][c]);
+                    Y[r][c] = yn;
+                }
+            if (change < 1e-13) break;  /* quadratic convergence: the next step is below rounding */
+        }
+        k++;
+    }
+    /* log Y = 2 atanh(Z), Z = (Y - I)(Y + I)^-1 */
+    cm3 A, B, Z2, term;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            A[r][c] = Y[r][c] - (r == c ? 1.0 : 0.0);
+            B[r][c] = Y[r][c] + (r == c ? 1.0 : 0.0);
+        }
+    cm3_inv(B, B);
+    cm3_mul(A, B, Z);
+    cm3_mul(Z, Z, Z2);
+    memcpy(term, Z, sizeof(cm3));
+    memcpy(L, Z, sizeof(cm3));
+    for (int n = 3; n < 200; n += 2) {
+        cm3_mul(term, Z2, term);
+        double tn = 0;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                L[r][c] += term[r][c] / n;
+                tn += cabs(term[r][c]);
+            }
+        if (tn / n < 1e-18) break;
+    }
+    double scale = 2.0 * ldexp(1.0, k);
+    double complex tr = 0;
+    for (int r = 0; r < 3; r++) tr += L[r][r];
+    if (fabs(cimag(tr) * scale) > 1.0) {  /* eigenphases adding up to +-2 pi */
+        su3_log_eigen(u, v);
+        return;
+    }
+    double vals[18];
+    /* H = -i log U */
+    for (int i = 0; i < 9; i++) {
+        double complex h = -I * L[i / 3][i % 3] * scale;
+        vals[i] = creal(h);
+        vals[9 + i] = cimag(h);
+    }
+    su3_hermiticize(vals, v);
+}
+
+/* the generator components of getAlgebraElement (SU(3)) */
+void orc_su3_log_gen(const double *u, double *gen)
+{
+    double v[9];
+    su3_log(u, v);
+    su3_to_gen(v, gen);
 }
 
 /* ---- generic dispatch ---- */
@@ -1750,78 +1975,105 @@ static void su2_link_ref(const double *v, double *u)
 /* CoulombGauge.CalculateDivergence (:148-166) for every colour: div[c][x] =
  * sum_dir A_c(U_dir(x)) - A_c(U_dir(x - dir)); returns the sum of squares in the
  * reference's order (colour by colour, cells in sequence). */
+/* generator components of getAlgebraElement (SU(2): 2 asin|e| e_a/|e|; SU(3): su3_log) */
+static int link_log_gen(int nc, const double *u, double *g)
+{
+    if (nc == 2) { su2_log(u, g); return 3; }
+    orc_su3_log_gen(u, g);
+    return 8;
+}
+
+/* CoulombGauge.CalculateDivergence (CoulombGauge.java:148-166) per colour c of
+ * the gauge field A = getAlgebraElement(U) (generator components); div: [ncomp][V] */
 double orc_coulomb_divergence(const orc_params *p, const double *U, double *div)
 {
     long V = vol(p);
+    int nc = p->nc, ng = orc_ng(nc), ncomp = nc == 2 ? 3 : 8;
+    double *A = malloc(sizeof(double) * (size_t)V * 3 * ncomp);
+    for (long x = 0; x < V; x++)
+        for (int dir = 0; dir < 3; dir++) link_log_gen(nc, U + ((size_t)x * 3 + dir) * ng, A + ((size_t)x * 3 + dir) * ncomp);
     double total = 0.0;
-    for (int c = 0; c < 3; c++) {
+    for (int c = 0; c < ncomp; c++) {
         double s = 0.0;
         for (long x = 0; x < V; x++) {
             double d = 0.0;
             for (int dir = 0; dir < 3; dir++) {
-                double a[3], b[3];
-                su2_log(link(p, U, x, dir), a);
-                su2_log(link(p, U, orc_shift(p, x, dir, -1), dir), b);
-                d += a[c] - b[c];
+                long xs = orc_shift(p, x, dir, -1);
+                d += A[((size_t)x * 3 + dir) * ncomp + c] - A[((size_t)xs * 3 + dir) * ncomp + c];
             }
             div[(size_t)c * V + x] = d;
             s += d * d;
         }
         total += s;
     }
+    free(A);
     return total;
 }
 
 /* g(x) = getLink(-psi(x)) (CoulombGauge.java:114-122) and GaugeTransformation's
- * action (GaugeTransformation.java:57-90) on U, Unext and E.  psi: [3][V]. */
+ * action (GaugeTransformation.java:57-90) on U, Unext and E.  psi: [ncomp][V]. */
 void orc_coulomb_apply(const orc_params *p, const double *psi, double *U, double *Unext, double *E)
 {
     long V = vol(p);
-    double *g = malloc(sizeof(double) * 4 * V);
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc), ncomp = nc == 2 ? 3 : 8;
+    double *g = malloc(sizeof(double) * ng * V);
     for (long x = 0; x < V; x++) {
-        double v[3] = {psi[x] * -1, psi[V + x] * -1, psi[2 * V + x] * -1};
-        su2_link_ref(v, g + 4 * x);
+        double v[8], alg[9];
+        for (int c = 0; c < ncomp; c++) v[c] = psi[(size_t)c * V + x] * -1;
+        if (nc == 2) su2_link_ref(v, g + 4 * x);
+        else { su3_from_gen(v, alg); su3_getlink(alg, g + 18 * x); }
     }
     for (long x = 0; x < V; x++)
         for (int dir = 0; dir < 3; dir++) {
-            double gd[4], t[4], r[4];
+            double gd[NG_MAX], t[NG_MAX], r[NG_MAX];
             long xs = orc_shift(p, x, dir, 1);
-            orc_group_adj(2, g + 4 * xs, gd);
-            double *u = U + ((size_t)x * 3 + dir) * 4;
-            orc_group_mult(2, g + 4 * x, u, t);
-            orc_group_mult(2, t, gd, r);
-            memcpy(u, r, sizeof(r));
-            u = Unext + ((size_t)x * 3 + dir) * 4;
-            orc_group_mult(2, g + 4 * x, u, t);
-            orc_group_mult(2, t, gd, r);
-            memcpy(u, r, sizeof(r));
-            /* E -> proj(g getLinearizedLink(E) g^dagger) (SU2AlgebraElement.java:133-138) */
-            double *e = E + ((size_t)x * 3 + dir) * 3;
-            double sum = (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) / 4;
-            double L[4] = {sqrt(1.0 - sum), e[0] / 2, e[1] / 2, e[2] / 2}, ga[4];
-            orc_group_adj(2, g + 4 * x, ga);
-            orc_group_mult(2, g + 4 * x, L, t);
-            orc_group_mult(2, t, ga, r);
-            orc_group_proj(2, r, e);
+            const double *gx = g + (size_t)ng * x;
+            orc_group_adj(nc, g + (size_t)ng * xs, gd);
+            double *u = U + ((size_t)x * 3 + dir) * ng;
+            orc_group_mult(nc, gx, u, t);
+            orc_group_mult(nc, t, gd, r);
+            memcpy(u, r, sizeof(double) * ng);
+            u = Unext + ((size_t)x * 3 + dir) * ng;
+            orc_group_mult(nc, gx, u, t);
+            orc_group_mult(nc, t, gd, r);
+            memcpy(u, r, sizeof(double) * ng);
+            /* E -> proj(g getLinearizedLink(E) g^dagger) (SU2AlgebraElement.java:133-138,
+             * SU3AlgebraElement.java:402-405) */
+            double *e = E + ((size_t)x * 3 + dir) * na;
+            double Lk[NG_MAX], ga[NG_MAX];
+            if (nc == 2) {
+                double sum = (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) / 4;
+                Lk[0] = sqrt(1.0 - sum); Lk[1] = e[0] / 2; Lk[2] = e[1] / 2; Lk[3] = e[2] / 2;
+            } else {
+                double w[18] = {1, e[3], e[6], -e[3], 1, e[7], -e[6], -e[7], 1,
+                                e[0], e[1], e[2], e[1], e[4], e[5], e[2], e[5], e[8]};
+                memcpy(Lk, w, sizeof(w));
+            }
+            orc_group_adj(nc, gx, ga);
+            orc_group_mult(nc, gx, Lk, t);
+            orc_group_mult(nc, t, ga, r);
+            orc_group_proj(nc, r, e);
         }
     free(g);
 }
 
 /* The gauge field of OccupationNumbersInTime.calculate (:203-225):
  * A[dir][c][x] = 0.5 (A_c(U_dir(x)) + A_c(Unext_dir(x))) * gainv and
- * Ef[dir][c][x] = E_dir(x)_c * gainv. */
+ * Ef[dir][c][x] = E_dir(x).get(c) * gainv, c over the ncomp generator components. */
 void orc_occupation_fields(const orc_params *p, const double *U, const double *Unext, const double *E,
                            double gainv, double *Ef, double *A)
 {
     long V = vol(p);
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc), ncomp = nc == 2 ? 3 : 8;
     for (long x = 0; x < V; x++)
         for (int j = 0; j < 3; j++) {
-            double a0[3], a1[3];
-            su2_log(link(p, U, x, j), a0);
-            su2_log(link(p, Unext, x, j), a1);
-            for (int k = 0; k < 3; k++) {
-                Ef[((size_t)j * 3 + k) * V + x] = E[((size_t)x * 3 + j) * 3 + k] * gainv;
-                A[((size_t)j * 3 + k) * V + x] = 0.5 * (a0[k] * gainv + a1[k] * gainv);
+            double a0[8], a1[8], eg[8];
+            link_log_gen(nc, U + ((size_t)x * 3 + j) * ng, a0);
+            link_log_gen(nc, Unext + ((size_t)x * 3 + j) * ng, a1);
+            orc_alg_to_gen(nc, E + ((size_t)x * 3 + j) * na, eg);
+            for (int k = 0; k < ncomp; k++) {
+                Ef[((size_t)j * ncomp + k) * V + x] = eg[k] * gainv;
+                A[((size_t)j * ncomp + k) * V + x] = 0.5 * (a0[k] * gainv + a1[k] * gainv);
             }
         }
 }

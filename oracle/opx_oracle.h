@@ -150,6 +150,8 @@ void orc_mv_charges(const orc_params *p, int direction, double location, double 
 /* LightConePoissonSolverImproved.solve after the Poisson solves */
 void orc_cgc_solve(const orc_params *p, int direction, int orientation, const double *phi,
                    double *U, double *Unext, double *E, const uint8_t *active, double *gauss, double *vt);
+/* SU3GroupElement.getAlgebraElement in generator components (own eigen-decomposition) */
+void orc_su3_log_gen(const double *u, double *gen);
 /* WilsonLineObservables (vt: V at the boundary behind the nucleus, [ntr][ng]) */
 double orc_wilson_tadpole(int nc, const double *vt, long ntr);
 int orc_wilson_dipole(int nc, const double *vt, int n1, int n2, double a1, double a2, double *out, double *ds_out);

@@ -119,3 +119,108 @@ def test_mirror_roundtrip_and_windows(orc):
     xx = (x0 * 1.0 - 2.0) / 4.0
     plateau = np.abs(xx) <= 0.25
     assert np.allclose(t.E[plateau], g.E[plateau], rtol=0, atol=0)
+
+
+def _su3_from_herm(H):
+    """exp(i H) for a 3x3 hermitian H, as 18 reals (re, im row-major)."""
+    import scipy.linalg
+    U = scipy.linalg.expm(1j * H)
+    return np.concatenate([U.real.reshape(-1), U.imag.reshape(-1)])
+
+
+def _gen_herm(x):
+    """H = x_a lambda_a / 2 (Gell-Mann matrices)."""
+    lam = np.zeros((8, 3, 3), complex)
+    lam[0][0, 1] = lam[0][1, 0] = 1
+    lam[1][0, 1], lam[1][1, 0] = -1j, 1j
+    lam[2][0, 0], lam[2][1, 1] = 1, -1
+    lam[3][0, 2] = lam[3][2, 0] = 1
+    lam[4][0, 2], lam[4][2, 0] = -1j, 1j
+    lam[5][1, 2] = lam[5][2, 1] = 1
+    lam[6][1, 2], lam[6][2, 1] = -1j, 1j
+    lam[7] = np.diag([1, 1, -2]) / np.sqrt(3)
+    return np.einsum("a,aij->ij", x, lam) / 2
+
+
+@pytest.mark.parametrize("scale", [1e-6, 0.05, 0.8, 2.5])
+def test_su3_log_inverts_exp(orc, scale):
+    """The oracle's SU(3) logarithm (SU3GroupElement.getAlgebraElement) returns
+    the generator components x with exp(i x_a lambda_a / 2) = U: for random x
+    of the given size (principal branch, |x| below pi) the components come back
+    to 1e-12, near the identity too."""
+    import ctypes as C
+    from oracle import _p, lib
+    L = lib()
+    L.orc_su3_log_gen.argtypes = [C.c_void_p, C.c_void_p]
+    rng = np.random.default_rng(11)
+    for _ in range(50):
+        x = rng.normal(size=8)
+        x *= scale / np.linalg.norm(x)
+        u = _su3_from_herm(_gen_herm(x))
+        g = np.empty(8)
+        L.orc_su3_log_gen(_p(u), _p(g))
+        assert np.abs(g - x).max() <= 1e-12 * max(1.0, scale), (x, g)
+
+
+def test_su3_log_degenerate(orc):
+    """Coincident eigenvalues: diag(e^{ia}, e^{ia}, e^{-2ia}) conjugated by a
+    random unitary, and the identity."""
+    import ctypes as C
+    import scipy.stats
+    from oracle import _p, lib
+    L = lib()
+    L.orc_su3_log_gen.argtypes = [C.c_void_p, C.c_void_p]
+    W = scipy.stats.unitary_group.rvs(3, random_state=4)
+    for a in (0.0, 0.3, 1.0):
+        H = W @ np.diag([a, a, -2 * a]) @ W.conj().T
+        u = _su3_from_herm(H)
+        g = np.empty(8)
+        L.orc_su3_log_gen(_p(u), _p(g))
+        assert np.abs(_gen_herm(g) - H).max() <= 1e-12, a
+
+
+def test_su3_log_phase_sum_2pi(orc):
+    """Eigenphases whose principal values add up to 2 pi: the logarithm is
+    still traceless and exp(i H) = U (one phase carries the 2 pi)."""
+    import ctypes as C
+    import scipy.linalg
+    import scipy.stats
+    from oracle import _p, lib
+    L = lib()
+    L.orc_su3_log_gen.argtypes = [C.c_void_p, C.c_void_p]
+    W = scipy.stats.unitary_group.rvs(3, random_state=7)
+    H0 = W @ np.diag([2.3, 2.2, -4.5]) @ W.conj().T
+    u = _su3_from_herm(H0)
+    g = np.empty(8)
+    L.orc_su3_log_gen(_p(u), _p(g))
+    H = _gen_herm(g)
+    assert abs(np.trace(H)) < 1e-12
+    U1 = scipy.linalg.expm(1j * H)
+    U0 = (u[:9] + 1j * u[9:]).reshape(3, 3)
+    assert np.abs(U1 - U0).max() < 1e-12
+
+
+def test_su3_coulomb_gauge_removes_pure_gauge(orc):
+    """SU(3): links U_i(x) = g(x) g(x+i)^dagger of a random gauge function g and
+    E = 0 are pure gauge; the Coulomb gauge iteration drives the divergence
+    below the goal and the occupation numbers and energy to zero."""
+    import ctypes as C
+    from oracle import _p, lib, occupation
+    g = orc.OracleGrid(3, (4, 5, 6), dt=0.1)
+    rng = np.random.default_rng(2)
+    V = g.V
+    G = np.empty((V, 18))
+    L = lib()
+    for x in range(V):
+        G[x] = _su3_from_herm(_gen_herm(rng.normal(0, 0.15, 8)))
+    def cm(v):
+        return (v[:9] + 1j * v[9:]).reshape(3, 3)
+    for x in range(V):
+        for d in range(3):
+            xs = g.shift(x, d, 1)
+            M = cm(G[x]) @ cm(G[xs]).conj().T
+            g.U[x, d] = np.concatenate([M.real.reshape(-1), M.imag.reshape(-1)])
+    g.Unext[...] = g.U
+    n, e, conv = occupation.occupation_numbers(g, max_iter=200, goal=1e-20)
+    assert conv[-1] < 1e-20
+    assert np.abs(n).max() < 1e-12 and abs(e) < 1e-12
