@@ -222,10 +222,11 @@ int opx_cgc_wilson_lines(opx_ctx *ctx, int nucleus, double *tadpole, double *dip
  * CoulombGauge.applyGaugeTransformation (physics/gauge/CoulombGauge.java:56-194;
  * at most max_iter iterations, until the summed squared divergence of
  * A = log U falls below accuracy_goal; the reference uses 100 and 1e-18),
- * then the occupation numbers n [V][3] (momentum index in cell order, colour
- * inner) and the energy density from them.  n_out may be NULL.  SU(2), one
- * lattice spacing.  opx_occupation_numbers_ex adds the mirrored grid and the
- * cone windows. */
+ * then the occupation numbers n [V][N^2 - 1] (momentum index in cell order, colour
+ * inner) and the energy density from them.  n_out may be
+ * NULL.  SU(2) and SU(3) (the SU(3) gauge field from the matrix logarithm of
+ * SU3GroupElement.getAlgebraElement), one lattice spacing.
+ * opx_occupation_numbers_ex adds the mirrored grid and the cone windows. */
 int opx_occupation_numbers(opx_ctx *ctx, int max_iter, double accuracy_goal, double *n_out, size_t count,
                            double *energy_density, int *iterations, double *last_divergence);
 

@@ -373,7 +373,7 @@ class Handle:
         """OccupationNumbersInTime: (n [V][3] or None, energy density, iterations,
         last divergence); the mirrored grid and the windows (WINDOW_* flags) as
         the diagnostic's options."""
-        n = np.empty((self.V, 3)) if with_n else None
+        n = np.empty((self.V, self.ngen)) if with_n else None
         e, it, dv = C.c_double(), C.c_int(), C.c_double()
         opt = OccupationOptions(int(mirrored_direction), int(windows), float(collision_time),
                                 (C.c_double * 3)(*collision_position), (C.c_double * 3)(*cone_velocity),

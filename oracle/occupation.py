@@ -150,14 +150,27 @@ def windows(g: OracleGrid, flags, time, ctime, cpos, cvel, tukey):
                     inside &= ~((pos < min_p) | (pos > max_p))
         if flag == CONE:
             out = ~inside
-            g.U[out] = np.array([1.0, 0.0, 0.0, 0.0])
-            g.Unext[out] = np.array([1.0, 0.0, 0.0, 0.0])
+            ident = np.zeros(g.U.shape[-1])
+            ident[[0, 4, 8] if g.nc == 3 else [0]] = 1.0
+            g.U[out] = ident
+            g.Unext[out] = ident
             g.E[out] = 0.0
         else:
             g.E *= factor[:, None, None]
-            f3 = np.repeat(factor[:, None], 3, 1)
-            g.U[...] = _su2_pow(g.U, f3)
-            g.Unext[...] = _su2_pow(g.Unext, f3)
+            if g.nc == 2:
+                f3 = np.repeat(factor[:, None], 3, 1)
+                g.U[...] = _su2_pow(g.U, f3)
+                g.Unext[...] = _su2_pow(g.Unext, f3)
+            else:
+                L = lib()
+                L.orc_su3_pow.argtypes = [C.c_void_p, C.c_double, C.c_void_p]
+                for arr in (g.U, g.Unext):
+                    for site in range(g.V):
+                        for d in range(3):
+                            u = np.ascontiguousarray(arr[site, d])
+                            o = np.empty(18)
+                            L.orc_su3_pow(_p(u), float(factor[site]), _p(o))
+                            arr[site, d] = o
 
 
 def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18, mirrored_direction=-1, window_flags=0,
@@ -175,8 +188,6 @@ def occupation_numbers(grid: OracleGrid, max_iter=100, goal=1e-18, mirrored_dire
         g = grid.copy()
         conv = coulomb_gauge(g, max_iter, goal)
     if window_flags:
-        if g.nc != 2:
-            raise ValueError("the windows take SU(2) powers of the links")
         windows(g, window_flags, time, collision_time, collision_position, cone_velocity, tukey_width)
     V, dims = g.V, g.dims
     ncomp = 3 if g.nc == 2 else 8

@@ -545,6 +545,15 @@ void orc_su3_log_gen(const double *u, double *gen)
     su3_to_gen(v, gen);
 }
 
+/* SU3GroupElement.pow(x) = getAlgebraElement().mult(x).getLink() (math/SU3GroupElement.java:516-518) */
+void orc_su3_pow(const double *u, double x, double *out)
+{
+    double v[9];
+    su3_log(u, v);
+    for (int k = 0; k < 9; k++) v[k] *= x;
+    su3_getlink(v, out);
+}
+
 /* ---- generic dispatch ---- */
 void orc_group_mult(int nc, const double *l, const double *r, double *out)
 {

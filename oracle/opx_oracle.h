@@ -152,6 +152,7 @@ void orc_cgc_solve(const orc_params *p, int direction, int orientation, const do
                    double *U, double *Unext, double *E, const uint8_t *active, double *gauss, double *vt);
 /* SU3GroupElement.getAlgebraElement in generator components (own eigen-decomposition) */
 void orc_su3_log_gen(const double *u, double *gen);
+void orc_su3_pow(const double *u, double x, double *out);
 /* WilsonLineObservables (vt: V at the boundary behind the nucleus, [ntr][ng]) */
 double orc_wilson_tadpole(int nc, const double *vt, long ntr);
 int orc_wilson_dipole(int nc, const double *vt, int n1, int n2, double a1, double a2, double *out, double *ds_out);

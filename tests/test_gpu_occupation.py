@@ -66,10 +66,15 @@ def test_occupation_numbers_vs_oracle(native, orc):
     assert abs(e32 - e_ref) <= 1e-5 * abs(e_ref)
 
 
-def test_occupation_rejects_su3(native):
+def test_occupation_rejects_bad_options(native):
     h = opx.Handle(3, (4, 4, 4))
     with pytest.raises(opx.OpixiError):
-        h.occupation_numbers()
+        h.occupation_numbers(mirrored_direction=3)
+    with pytest.raises(opx.OpixiError):
+        h.occupation_numbers(windows=8)
+    h2 = opx.Handle(2, (4, 4, 4), a=(1.0, 1.0, 0.5))
+    with pytest.raises(opx.OpixiError):
+        h2.occupation_numbers()  # one lattice spacing only, as in the reference
 
 
 OPTION_CASES = {
@@ -106,6 +111,42 @@ def test_occupation_options_vs_oracle(native, orc, case):
     n_ref, e_ref, conv = occupation.occupation_numbers(g, time=6 * 0.5, **opt)
     kw = {("windows" if k == "window_flags" else k): v for k, v in opt.items()}
     n, e, it, dv = h.occupation_numbers(**kw)
+    assert it == len(conv)
+    assert np.abs(n - n_ref).max() <= 1e-9 * np.abs(n_ref).max()
+    assert abs(e - e_ref) <= 1e-10 * abs(e_ref)
+
+
+SU3_CASES = {
+    "plain": dict(),
+    "mirrored_1": dict(mirrored_direction=1),
+    "gaussian_cone": dict(window_flags=5, collision_time=0.0, collision_position=(3.0, 2.0, 3.0),
+                          cone_velocity=(1.0, 0.0, 1.0)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(SU3_CASES))
+def test_su3_occupation_vs_oracle(native, orc, case):
+    """SU(3): the Coulomb gauge with the SU(3) logarithm and the occupation
+    numbers (8 colours), with the mirrored grid and the windows, against the
+    oracle: n within 1e-9 of the largest, energy 1e-10, the same iterations."""
+    from oracle import occupation
+    opt = SU3_CASES[case]
+    g = orc.OracleGrid(3, (6, 5, 7), dt=0.5, g=1.2)
+    g.random_links(9, 0.2)
+    g.random_e(9, 0.15)
+    g.update_links()
+    h = opx.Handle(3, g.dims, a=g.a, dt=g.dt, g=g.g, precision=N.OPX_F64)
+    h.upload(N.FIELD_U, g.U)
+    h.upload(N.FIELD_UNEXT, g.Unext)
+    h.upload(N.FIELD_E, g.E)
+    h.step(4)
+    g.U[...] = h.download(N.FIELD_U)
+    g.Unext[...] = h.download(N.FIELD_UNEXT)
+    g.E[...] = h.download(N.FIELD_E)
+    n_ref, e_ref, conv = occupation.occupation_numbers(g, max_iter=60, goal=1e-16, time=4 * 0.5, **opt)
+    kw = {("windows" if k == "window_flags" else k): v for k, v in opt.items()}
+    n, e, it, dv = h.occupation_numbers(max_iter=60, accuracy_goal=1e-16, **kw)
+    assert n.shape == (g.V, 8)
     assert it == len(conv)
     assert np.abs(n - n_ref).max() <= 1e-9 * np.abs(n_ref).max()
     assert abs(e - e_ref) <= 1e-10 * abs(e_ref)
