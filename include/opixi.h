@@ -138,7 +138,7 @@ int opx_update_grid(opx_ctx *ctx);
 /* Field solver of opx_update_grid / opx_step (Settings.applySimulationTypeSetting,
  * physics/Settings.java:540-581): FastTYMSolver (the default), or
  * ImplicitTYMSolver(implicitSolverIterations, implicitSolverDamping)
- * (physics/fields/ImplicitTYMSolver.java:35-58; SU(2)) for the implicit CGC types. */
+ * (physics/fields/ImplicitTYMSolver.java:35-58; SU(2), SU(3)) for the implicit CGC types. */
 #define OPX_SOLVER_FAST 0
 #define OPX_SOLVER_IMPLICIT 1
 int opx_set_field_solver(opx_ctx *ctx, int kind, int iterations, double damping);

@@ -436,7 +436,6 @@ int opx_set_field_solver(opx_ctx *ctx, int kind, int iterations, double damping)
         c.err = "opx_set_field_solver: kind FAST or IMPLICIT, iterations >= 0, 0 <= damping <= 1";
         return OPX_ERR_INVALID;
     }
-    if (c.nc != 2) { c.err = "opx_set_field_solver: the implicit solver is provided for SU(2)"; return OPX_ERR_UNSUPPORTED; }
     c.imp_solver = true;
     c.imp_iterations = iterations;
     c.imp_damping = damping;

@@ -15,6 +15,7 @@
 // 0 are resident in L2 while a block works on its plane).
 #include "internal.h"
 #include "leapfrog.cuh"
+#include "su3_log.cuh"
 #include "su3_pair.cuh"
 
 namespace opx {
@@ -61,7 +62,7 @@ k_update_grid_su3f_pair(const float *__restrict__ U, float *__restrict__ E, cons
 
 // SU2GroupElement.pow(x) = exp(x log u) (math/SU2GroupElement.java:234-271)
 template <typename R>
-__device__ __forceinline__ Q2<R> su2_pow(const Q2<R> &u, R x) {
+__device__ __forceinline__ Q2<R> group_pow(const Q2<R> &u, R x) {
     R norm = u.e[1] * u.e[1] + u.e[2] * u.e[2] + u.e[3] * u.e[3];
     norm = Real<R>::sqrt_(norm);
     R v[3];
@@ -74,16 +75,28 @@ __device__ __forceinline__ Q2<R> su2_pow(const Q2<R> &u, R x) {
     for (int c = 0; c < 3; c++) v[c] *= x;
     return SU2<R>::expi(v);
 }
+// SU3GroupElement.pow(x) = getAlgebraElement().mult(x).getLink() (math/SU3GroupElement.java:516-518);
+// the logarithm in FP64 (su3_log.cuh)
+template <typename R>
+__device__ __forceinline__ M3<R> group_pow(const M3<R> &u, R x) {
+    M3<double> ud;
+    for (int k = 0; k < 9; k++) { ud.r[k] = (double)u.r[k]; ud.i[k] = (double)u.i[k]; }
+    double g[8];
+    su3_log_gen(ud, g);
+    R v[8];
+    for (int a = 0; a < 8; a++) v[a] = (R)(g[a] * (double)x);
+    return SU3<R>::expi(v);
+}
 
 // ImplicitStep.getPlaquetteSum (:136-177): links of direction i / d at time
 // -1 (Wm: the grid's Unext slot = the previous links), 0 (W0 = grid U) or +1
 // (Wp = Ui), implicit time in the transverse plane and along the beam (0).
-template <typename R>
-__device__ __forceinline__ Q2<R> implicit_psum(const LinkPlanes<SU2<R>, R> &Wm, const LinkPlanes<SU2<R>, R> &W0,
-                                               const LinkPlanes<SU2<R>, R> &Wp, const Lat &L, long s, const int *x,
-                                               int d, int time) {
-    using G = SU2<R>;
-    Q2<R> S = G::zero();
+template <class G, typename R>
+__device__ __forceinline__ typename G::M implicit_psum(const LinkPlanes<G, R> &Wm, const LinkPlanes<G, R> &W0,
+                                                       const LinkPlanes<G, R> &Wp, const Lat &L, long s, const int *x,
+                                                       int d, int time) {
+    using M = typename G::M;
+    M S = G::zero();
     const int beam = 0;
     const long ci1 = shift_d(L, s, x[d], d, +1);
     int x1[3] = {x[0], x[1], x[2]};
@@ -99,8 +112,8 @@ __device__ __forceinline__ Q2<R> implicit_psum(const LinkPlanes<SU2<R>, R> &Wm, 
         const LinkPlanes<G, R> &Wi = ti < 0 ? Wm : (ti > 0 ? Wp : W0);
         const long ci2 = shift_d(L, s, x[i], i, +1), ci3 = shift_d(L, ci1, x1[i], i, -1),
                    ci4 = shift_d(L, s, x[i], i, -1);
-        Q2<R> U1 = G::mul_adj(G::mul_adj(Wi.load(i, ci1), Wd.load(d, ci2)), Wi.load(i, s));
-        const Q2<R> U2 = G::mul(G::adj(G::mul(Wd.load(d, ci4), Wi.load(i, ci3))), Wi.load(i, ci4));
+        M U1 = G::mul_adj(G::mul_adj(Wi.load(i, ci1), Wd.load(d, ci2)), Wi.load(i, s));
+        const M U2 = G::adj_mul(G::mul(Wd.load(d, ci4), Wi.load(i, ci3)), Wi.load(i, ci4));
         G::add(U1, U2);
         U1 = G::mul(Wd.load(d, s), U1);
         G::scale(U1, LatR<R>::inva2(L, i));
@@ -110,62 +123,65 @@ __device__ __forceinline__ Q2<R> implicit_psum(const LinkPlanes<SU2<R>, R> &Wm, 
 }
 
 // ImplicitStep (:103-131) fused with ImplicitDamping (:195-207) for the three links of a site
-template <typename R, bool HAS_J>
+template <int NC, typename R, bool HAS_J>
 __global__ void __launch_bounds__(128) k_implicit_step(const R *__restrict__ U, const R *__restrict__ Uprev,
                                                        const R *__restrict__ Ui, const R *__restrict__ E,
                                                        const R *__restrict__ J, R *__restrict__ Ei,
                                                        R *__restrict__ Uin, const uint8_t *__restrict__ active, Lat L,
                                                        R damping) {
-    using G = SU2<R>;
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
     const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.V) return;
     if (active && !active[s]) return;
     const LinkPlanes<G, R> Wm{const_cast<R *>(Uprev), L.V}, W0{const_cast<R *>(U), L.V}, Wp{const_cast<R *>(Ui), L.V},
         Wn{Uin, L.V};
-    const AlgPlanes<3, R> Ep{const_cast<R *>(E), L.V}, Eo{Ei, L.V}, Jp{const_cast<R *>(J), L.V};
+    const AlgPlanes<NA, R> Ep{const_cast<R *>(E), L.V}, Eo{Ei, L.V}, Jp{const_cast<R *>(J), L.V};
     int x[3];
     site_coords(L, s, x);
     const R dt = LatR<R>::dt(L), hdt = dt * R(0.5);
 #pragma unroll 1
     for (int i = 0; i < 3; i++) {
-        R e[3], pr[3];
+        R e[NA], pr[NA];
         Ep.load_ro(i, s, e);
-        G::proj(implicit_psum(Wm, W0, Wp, L, s, x, i, +1), pr);
-        for (int c = 0; c < 3; c++) e[c] += pr[c] * hdt;
-        G::proj(implicit_psum(Wm, W0, Wp, L, s, x, i, -1), pr);
-        for (int c = 0; c < 3; c++) e[c] += pr[c] * hdt;
+        G::proj(implicit_psum<G, R>(Wm, W0, Wp, L, s, x, i, +1), pr);
+        for (int c = 0; c < NA; c++) e[c] += pr[c] * hdt;
+        G::proj(implicit_psum<G, R>(Wm, W0, Wp, L, s, x, i, -1), pr);
+        for (int c = 0; c < NA; c++) e[c] += pr[c] * hdt;
         if (HAS_J) {
-            R jv[3];
+            R jv[NA];
             Jp.load_ro(i, s, jv);
             const R jf = LatR<R>::jfac(L, i);
-            for (int c = 0; c < 3; c++) e[c] += jv[c] * jf;
+            for (int c = 0; c < NA; c++) e[c] += jv[c] * jf;
         }
         Eo.store(i, s, e);
-        R v[3];
-        for (int c = 0; c < 3; c++) v[c] = -dt * e[c];
-        const Q2<R> Vn = G::mul(G::expi(v), W0.load(i, s));
-        Wn.store(i, s, G::mul(su2_pow(Wp.load(i, s), damping), su2_pow(Vn, R(1) - damping)));
+        R v[NA];
+        for (int c = 0; c < NA; c++) v[c] = -dt * e[c];
+        const auto Vn = G::mul(G::expi(v), W0.load(i, s));
+        Wn.store(i, s, G::mul(group_pow(Wp.load(i, s), damping), group_pow(Vn, R(1) - damping)));
     }
 }
 
 // ImplicitEnd (:217-226): E and Unext of the active cells from the implicit grid
-template <typename R>
+template <int NC, typename R>
 __global__ void k_implicit_end(const R *__restrict__ Ei, const R *__restrict__ Uin, R *__restrict__ E,
                                R *__restrict__ Un, const uint8_t *__restrict__ active, Lat L) {
+    using G = typename GroupOf<NC, R>::T;
+    constexpr int NA = G::NA;
     const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.V) return;
     if (active && !active[s]) return;
-    const LinkPlanes<SU2<R>, R> A{const_cast<R *>(Uin), L.V}, B{Un, L.V};
+    const LinkPlanes<G, R> A{const_cast<R *>(Uin), L.V}, B{Un, L.V};
     for (int d = 0; d < 3; d++) {
         B.store(d, s, A.load(d, s));
-        for (int a = 0; a < 3; a++) E[((long)d * 3 + a) * L.V + s] = Ei[((long)d * 3 + a) * L.V + s];
+        for (int a = 0; a < NA; a++) E[((long)d * NA + a) * L.V + s] = Ei[((long)d * NA + a) * L.V + s];
     }
 }
 
-template <typename R>
+template <int NC, typename R>
 static int implicit_update_t(Ctx &c) {
     const long V = c.L.V;
-    const size_t nU = (size_t)link_elems(V, 4) * sizeof(R), nE = (size_t)V * 9 * sizeof(R);
+    const size_t nU = (size_t)link_elems(V, c.ng) * sizeof(R), nE = (size_t)V * 3 * c.na * sizeof(R);
     if (!c.imp_Ua) {
         if (cudaMalloc(&c.imp_Ua, nU) != cudaSuccess || cudaMalloc(&c.imp_Ub, nU) != cudaSuccess ||
             cudaMalloc(&c.imp_E, nE) != cudaSuccess) {
@@ -182,27 +198,27 @@ static int implicit_update_t(Ctx &c) {
     // ImplicitBegin (:68-90): the explicit combined update into the implicit grid
     const int B = 128;
     const dim3 grid(grid_for(V, B));
-    if (c.j_nonzero) k_update_grid<2, R, true, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
-    else k_update_grid<2, R, false, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
+    if (c.j_nonzero) k_update_grid<NC, R, true, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
+    else k_update_grid<NC, R, false, false, long><<<grid, B, 0, c.stream>>>((const R *)c.U, Ei, (const R *)c.J, Uin, c.active, c.L);
     c.launches++;
     for (int it = 0; it < c.imp_iterations; it++) {
         std::swap(Ui, Uin);  // implicitGrid.storeFields()
         if (c.j_nonzero)
-            k_implicit_step<R, true><<<grid, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, Ui, (const R *)c.E,
+            k_implicit_step<NC, R, true><<<grid, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, Ui, (const R *)c.E,
                                                                (const R *)c.J, Ei, Uin, c.active, c.L, (R)c.imp_damping);
         else
-            k_implicit_step<R, false><<<grid, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, Ui, (const R *)c.E,
+            k_implicit_step<NC, R, false><<<grid, B, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, Ui, (const R *)c.E,
                                                                 (const R *)c.J, Ei, Uin, c.active, c.L, (R)c.imp_damping);
         c.launches++;
     }
-    k_implicit_end<R><<<grid, B, 0, c.stream>>>(Ei, Uin, (R *)c.E, (R *)c.Unext, c.active, c.L);
+    k_implicit_end<NC, R><<<grid, B, 0, c.stream>>>(Ei, Uin, (R *)c.E, (R *)c.Unext, c.active, c.L);
     c.launches++;
     return OPX_OK;
 }
 
 int launch_implicit_update(Ctx &c) {
-    if (c.nc != 2) { c.err = "implicit solver: SU(2) only"; return OPX_ERR_UNSUPPORTED; }
-    return c.prec == OPX_F64 ? implicit_update_t<double>(c) : implicit_update_t<float>(c);
+    if (c.nc == 2) return c.prec == OPX_F64 ? implicit_update_t<2, double>(c) : implicit_update_t<2, float>(c);
+    return c.prec == OPX_F64 ? implicit_update_t<3, double>(c) : implicit_update_t<3, float>(c);
 }
 
 template <int NC, typename R>

@@ -165,7 +165,7 @@ class ProjectedEnergyDensity(Diagnostics):
 
 class OccupationNumbersInTime(Diagnostics):
     """diagnostics/methods/OccupationNumbersInTime.java: occupation numbers in
-    Coulomb gauge (SU(2)).  CSV output: a header with the grid size
+    Coulomb gauge (SU(2), SU(3)).  CSV output: a header with the grid size
     (+ the momentum vectors for "csv_with_vectors"), then per measurement
     "time, energy" and the occupation numbers (one line per colour when
     colorful, else their colour sum); "csv_only_energy" writes the first line

@@ -197,7 +197,7 @@ class OracleGrid:
         lib().orc_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext), _p(self.active))
 
     def update_grid_implicit(self, iterations, damping):
-        """ImplicitTYMSolver.step (SU(2)) in place of update_grid."""
+        """ImplicitTYMSolver.step (SU(2), SU(3)) in place of update_grid."""
         rc = lib().orc_implicit_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),
                                             _p(self.active), int(iterations), C.c_double(damping))
         if rc != 0:

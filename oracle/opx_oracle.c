@@ -2088,7 +2088,7 @@ void orc_occupation_fields(const orc_params *p, const double *U, const double *U
 }
 
 /* ------------------------------------------------------------------------- */
-/* ImplicitTYMSolver.step (physics/fields/ImplicitTYMSolver.java:35-58), SU(2) */
+/* ImplicitTYMSolver.step (physics/fields/ImplicitTYMSolver.java:35-58), SU(2) and SU(3) */
 /* ------------------------------------------------------------------------- */
 
 /* SU2GroupElement.pow(x) = getAlgebraElement().mult(x).getLink() (math/SU2GroupElement.java:269-271) */
@@ -2100,6 +2100,11 @@ static void su2_pow(const double *u, double x, double *out)
     su2_link_ref(v, out);
 }
 
+static void group_pow(int nc, const double *u, double x, double *out)
+{
+    if (nc == 2) su2_pow(u, x, out); else orc_su3_pow(u, x, out);
+}
+
 /* ImplicitStep.getPlaquetteSum (:136-177): plaquettes closed along the central
  * link, with the links of direction i / d taken at time -1 (W_m, the grid's
  * Unext slot, which holds the previous U), 0 (W_0 = grid U) or +1 (W_p = the
@@ -2107,7 +2112,7 @@ static void su2_pow(const double *u, double x, double *out)
 static void implicit_plaquette_sum(const orc_params *p, const double *Wm, const double *W0, const double *Wp,
                                    long index, int d, int beam, int time, double *S)
 {
-    const int ng = 4;
+    const int nc = p->nc, ng = orc_ng(nc);
     memset(S, 0, sizeof(double) * ng);
     long ci1 = orc_shift(p, index, d, 1);
     for (int i = 0; i < 3; i++) {
@@ -2119,18 +2124,18 @@ static void implicit_plaquette_sum(const orc_params *p, const double *Wm, const 
         const double *Wd = td < 0 ? Wm : (td > 0 ? Wp : W0);
         const double *Wi = ti < 0 ? Wm : (ti > 0 ? Wp : W0);
         long ci2 = orc_shift(p, index, i, 1), ci3 = orc_shift(p, ci1, i, -1), ci4 = orc_shift(p, index, i, -1);
-        double U1[4], U2[4], t[4], adj[4];
-        orc_group_adj(2, link(p, Wd, ci2, d), adj);
-        orc_group_mult(2, link(p, Wi, ci1, i), adj, U1);
-        orc_group_adj(2, link(p, Wi, index, i), adj);
-        orc_group_mult(2, U1, adj, t);
-        memcpy(U1, t, sizeof(t));
-        orc_group_mult(2, link(p, Wd, ci4, d), link(p, Wi, ci3, i), U2);
-        orc_group_adj(2, U2, t);
-        orc_group_mult(2, t, link(p, Wi, ci4, i), U2);
+        double U1[NG_MAX], U2[NG_MAX], t[NG_MAX], adj[NG_MAX];
+        orc_group_adj(nc, link(p, Wd, ci2, d), adj);
+        orc_group_mult(nc, link(p, Wi, ci1, i), adj, U1);
+        orc_group_adj(nc, link(p, Wi, index, i), adj);
+        orc_group_mult(nc, U1, adj, t);
+        memcpy(U1, t, sizeof(double) * ng);
+        orc_group_mult(nc, link(p, Wd, ci4, d), link(p, Wi, ci3, i), U2);
+        orc_group_adj(nc, U2, t);
+        orc_group_mult(nc, t, link(p, Wi, ci4, i), U2);
         double areaFactor = 1.0 / pow(p->a[i], 2);
         for (int k = 0; k < ng; k++) U1[k] = U1[k] + U2[k];
-        orc_group_mult(2, link(p, Wd, index, d), U1, t);
+        orc_group_mult(nc, link(p, Wd, index, d), U1, t);
         for (int k = 0; k < ng; k++) U1[k] = t[k] * areaFactor;
         for (int k = 0; k < ng; k++) S[k] = S[k] + U1[k];
     }
@@ -2138,12 +2143,11 @@ static void implicit_plaquette_sum(const orc_params *p, const double *Wm, const 
 
 /* In place of orc_update_grid for the implicit solver: U current links, Unext
  * the previous links (the slot after storeFields), E, J; writes E and Unext of
- * the active cells.  Returns -1 for SU(3). */
+ * the active cells. */
 int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, const double *J, double *Unext,
                              const uint8_t *active, int iterations, double damping)
 {
-    if (p->nc != 2) return -1;
-    const int ng = 4, na = 3, beam = 0;
+    const int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc), beam = 0;
     long V = vol(p);
     size_t nl = (size_t)V * 3 * ng, ne = (size_t)V * 3 * na;
     /* Grid(grid): the implicit grid is a copy */
@@ -2155,19 +2159,19 @@ int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, co
     for (long x = 0; x < V; x++) {
         if (active && !active[x]) continue;
         for (int i = 0; i < 3; i++) {
-            double S[4], temp[4], pr[3], ve[3], Vl[4], t[4];
+            double S[NG_MAX], temp[NG_MAX], pr[NA_MAX], ve[NA_MAX], Vl[NG_MAX], t[NG_MAX];
             double unitFactor = -(p->g * p->a[i]) * p->dt;
             orc_staple_sum(p, U, x, i, S);
-            orc_group_mult(2, link(p, U, x, i), S, temp);
-            orc_group_proj(2, temp, pr);
+            orc_group_mult(nc, link(p, U, x, i), S, temp);
+            orc_group_proj(nc, temp, pr);
             double *e = Ei + ((size_t)x * 3 + i) * na;
             const double *j = J + ((size_t)x * 3 + i) * na;
             for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * p->dt;
             for (int c = 0; c < na; c++) e[c] = e[c] + j[c] * unitFactor;
             for (int c = 0; c < na; c++) ve[c] = e[c] * -p->dt;
-            orc_alg_getlink(2, ve, Vl);
-            orc_group_mult(2, Vl, link(p, U, x, i), t);
-            memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+            orc_alg_getlink(nc, ve, Vl);
+            orc_group_mult(nc, Vl, link(p, U, x, i), t);
+            memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(double) * ng);
         }
     }
     for (int it = 0; it < iterations; it++) {
@@ -2176,33 +2180,33 @@ int orc_implicit_update_grid(const orc_params *p, const double *U, double *E, co
         for (long x = 0; x < V; x++) {
             if (active && !active[x]) continue;
             for (int i = 0; i < 3; i++) {
-                double S[4], pr[3], ve[3], Vl[4], t[4];
+                double S[NG_MAX], pr[NA_MAX], ve[NA_MAX], Vl[NG_MAX], t[NG_MAX];
                 double unitFactor = -(p->g * p->a[i]) * p->dt;
                 double *e = Ei + ((size_t)x * 3 + i) * na;
                 const double *j = J + ((size_t)x * 3 + i) * na;
                 memcpy(e, E + ((size_t)x * 3 + i) * na, sizeof(double) * na);
                 implicit_plaquette_sum(p, Unext, U, Ui, x, i, beam, +1, S);
-                orc_group_proj(2, S, pr);
+                orc_group_proj(nc, S, pr);
                 for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * (p->dt * 0.5);
                 implicit_plaquette_sum(p, Unext, U, Ui, x, i, beam, -1, S);
-                orc_group_proj(2, S, pr);
+                orc_group_proj(nc, S, pr);
                 for (int c = 0; c < na; c++) e[c] = e[c] + pr[c] * (p->dt * 0.5);
                 for (int c = 0; c < na; c++) e[c] = e[c] + j[c] * unitFactor;
                 for (int c = 0; c < na; c++) ve[c] = e[c] * -p->dt;
-                orc_alg_getlink(2, ve, Vl);
-                orc_group_mult(2, Vl, link(p, U, x, i), t);
-                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+                orc_alg_getlink(nc, ve, Vl);
+                orc_group_mult(nc, Vl, link(p, U, x, i), t);
+                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(double) * ng);
             }
         }
         /* ImplicitDamping (:195-207) */
         for (long x = 0; x < V; x++) {
             if (active && !active[x]) continue;
             for (int i = 0; i < 3; i++) {
-                double U1[4], U2[4], t[4];
-                su2_pow(Uin + ((size_t)x * 3 + i) * ng, 1 - damping, U1);
-                su2_pow(Ui + ((size_t)x * 3 + i) * ng, damping, U2);
-                orc_group_mult(2, U2, U1, t);
-                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(t));
+                double U1[NG_MAX], U2[NG_MAX], t[NG_MAX];
+                group_pow(nc, Uin + ((size_t)x * 3 + i) * ng, 1 - damping, U1);
+                group_pow(nc, Ui + ((size_t)x * 3 + i) * ng, damping, U2);
+                orc_group_mult(nc, U2, U1, t);
+                memcpy(Uin + ((size_t)x * 3 + i) * ng, t, sizeof(double) * ng);
             }
         }
     }

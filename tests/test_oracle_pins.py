@@ -336,12 +336,13 @@ def test_poynting_rows_against_independent_matrices(orc):
         assert np.abs(ref).max() > 1e-4
 
 
-def test_implicit_solver_properties(orc):
+@pytest.mark.parametrize("nc", [2, 3])
+def test_implicit_solver_properties(orc, nc):
     """ImplicitTYMSolver (physics/fields/ImplicitTYMSolver.java): with no
     iterations it is the explicit FastTYMSolver update bit for bit (ImplicitBegin
     is the CombinedUpdate); with iterations and no damping the fixed-point
     iteration converges (successive iterates approach each other)."""
-    g = orc.OracleGrid(2, (6, 6, 6), dt=0.05)
+    g = orc.OracleGrid(nc, (6, 6, 6) if nc == 2 else (4, 4, 5), dt=0.05)
     g.random_links(3, 0.3)
     g.random_e(3, 0.3)
     g.gauss_project()
