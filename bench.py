@@ -10,8 +10,10 @@ updates).  ``value`` is timed with CUDA events on the handle's own stream over
 K steps with the fields resident in HBM (inputs are larger than L2: the links
 alone are 453 MB).  ``e2e`` is the same metric through the public C ABI with
 host buffers: upload of the initial U and E from pinned memory, the K steps
-each followed by the BulkQuantities reduction read back to the host, and the
-download of the final U and E, all inside the timed region;
+with the BulkQuantities row of every step read back to the host
+(opx_step_measured; ``e2e.step_then_reduce`` makes the same run as one
+opx_step + opx_reduce call pair per step), and the download of the final U
+and E, all inside the timed region;
 ``e2e.per_call_copy`` is FieldSolver.step as a per-call drop-in whose host grid
 stays authoritative (U and E copied in, E and Unext copied out on every call).
 
@@ -700,29 +702,49 @@ def main():
         h2 = make_handle(w, w["prec"], device)
         he = (h2.ng + h2.na_ref) * 8 * links
         obs_bytes = 13 * 8
-        dist.barrier()
-        t = time.perf_counter()
-        h2.upload(N.FIELD_U, U_host.array)
-        h2.upload(N.FIELD_E, E_host.array)
-        h2.initialize()
-        t_in = time.perf_counter()
-        for k in range(args.steps):
-            h2.step(1)
-            h2.reduce()
-        t_loop = time.perf_counter()
-        h2.download(N.FIELD_U, out=U_host.array)
-        h2.download(N.FIELD_E, out=E_host.array)
-        t_out = time.perf_counter()
-        el = t_out - t
-        el = dist.max(el)
-        e2e = {"value": world * links * args.steps / el, "unit": METRIC,
-               "upload_ms": (t_in - t) * 1e3, "loop_ms_per_step": (t_loop - t_in) * 1e3 / args.steps,
-               "download_ms": (t_out - t_loop) * 1e3,
-               "h2d_bytes_per_step": he / args.steps,
-               "d2h_bytes_per_step": obs_bytes + he / args.steps,
-               "note": "Simulation.step through the C ABI with the BulkQuantities observables (13 FP64 "
-                       "values) read back to the host after every step; initial U,E uploaded from pinned "
-                       "host memory and final U,E downloaded inside the timed region"}
+        def run(measured):
+            U0, E0 = U_host.array.copy(), E_host.array.copy()
+            dist.barrier()
+            t = time.perf_counter()
+            h2.upload(N.FIELD_U, U_host.array)
+            h2.upload(N.FIELD_E, E_host.array)
+            h2.initialize()
+            t_in = time.perf_counter()
+            if measured:
+                rows = h2.step_measured(args.steps)
+            else:
+                rows = []
+                for k in range(args.steps):
+                    h2.step(1)
+                    rows.append(h2.reduce())
+            t_loop = time.perf_counter()
+            h2.download(N.FIELD_U, out=U_host.array)
+            h2.download(N.FIELD_E, out=E_host.array)
+            t_out = time.perf_counter()
+            el = dist.max(t_out - t)
+            U_host.array[...] = U0
+            E_host.array[...] = E0
+            return {"value": world * links * args.steps / el, "unit": METRIC,
+                    "upload_ms": (t_in - t) * 1e3, "loop_ms_per_step": (t_loop - t_in) * 1e3 / args.steps,
+                    "download_ms": (t_out - t_loop) * 1e3,
+                    "h2d_bytes_per_step": he / args.steps,
+                    "d2h_bytes_per_step": obs_bytes + he / args.steps}, rows
+
+        plain, rows_p = run(False)
+        meas, rows_m = run(True)
+        # the two forms must report the same observables (FP32 rounding of the per-site terms)
+        dev = max(abs(a.e2_total + a.b2_total - b.e2_total - b.b2_total) / abs(b.e2_total + b.b2_total)
+                  for a, b in zip(rows_m, rows_p))
+        meas["energy_rel_diff_vs_step_then_reduce"] = dev
+        plain["note"] = ("opx_step(ctx, 1) then opx_reduce on every step (FieldSolver.step and "
+                         "BulkQuantitiesInTime as separate drop-in calls)")
+        e2e = dict(meas)
+        e2e["note"] = ("MainBatch's loop with BulkQuantitiesInTime every step through the C ABI "
+                       "(opx_step_measured: the BulkQuantities row of every step, 13 FP64 values, copied "
+                       "to pinned host memory as each step completes; the step kernel forms the per-site "
+                       "terms); initial U,E uploaded from pinned host memory and final U,E downloaded inside "
+                       "the timed region")
+        e2e["step_then_reduce"] = plain
         # FieldSolver.step as a per-call drop-in with the host grid authoritative:
         # every call uploads U and E and downloads E and Unext (reference layout, FP64 host arrays)
         ncall = max(3, min(args.steps, 20))

@@ -155,6 +155,18 @@ long opx_steps_done(const opx_ctx *ctx);
 
 /* ---- reductions / diagnostics ---- */
 int opx_reduce(opx_ctx *ctx, opx_observables *out);
+/* nsteps x {Simulation.step; BulkQuantitiesInTime.calculate} (MainBatch's loop
+ * with BulkQuantitiesInTime every step, Simulation.java:373-435,
+ * BulkQuantitiesInTime.java:83-121): out[k] holds what opx_reduce returns after
+ * the (k+1)-th step.  For SU(3) FP32 handles with the FastTYMSolver, no current,
+ * no masks and no particles, each step's kernel also forms the per-site
+ * BulkQuantities terms it can from what it loads (E^2 of the new E, B^2 of its
+ * input links, the transported E of the Gauss law, whose sum the next step
+ * forms) and one reduction follows the last step; the values agree with
+ * opx_step + opx_reduce to FP32 rounding of the per-site terms (the plaquettes
+ * are multiplied in another order, the sums run in another order).  Otherwise,
+ * and for nsteps = 1, it is exactly opx_step(ctx, 1) + opx_reduce per step. */
+int opx_step_measured(opx_ctx *ctx, int nsteps, opx_observables *out);
 /* EnergyDensity.ComponentComputation (diagnostics/methods/EnergyDensity.java:119-166): V doubles */
 int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count);
 /* ProjectedEnergyDensity.EnergyDensityComputation (ProjectedEnergyDensity.java:114-179):

@@ -45,7 +45,7 @@ EXPORTED = [
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
     "opx_particles_count", "opx_projected_poynting", "opx_cgc_mv_super", "opx_super_groups",
     "opx_super_download", "opx_super_upload", "opx_occupation_numbers", "opx_set_field_solver",
-    "opx_cgc_wilson_lines", "opx_occupation_numbers_ex",
+    "opx_cgc_wilson_lines", "opx_occupation_numbers_ex", "opx_step_measured",
 ]
 
 
@@ -115,6 +115,7 @@ def load(path=None):
         "opx_synchronize": (C.c_int, [vp]),
         "opx_steps_done": (C.c_long, [vp]),
         "opx_reduce": (C.c_int, [vp, C.POINTER(Observables)]),
+        "opx_step_measured": (C.c_int, [vp, C.c_int, C.POINTER(Observables)]),
         "opx_energy_density": (C.c_int, [vp, vp, sz]),
         "opx_projected_energy": (C.c_int, [vp, C.c_int, vp, sz]),
         "opx_gauss_field": (C.c_int, [vp, vp, sz]),
@@ -284,6 +285,13 @@ class Handle:
         o = Observables()
         self.check(self.L.opx_reduce(self.h, C.byref(o)))
         return o
+
+    def step_measured(self, n):
+        """n steps with BulkQuantities after each: a list of n Observables (what
+        reduce() returns after each step)."""
+        out = (Observables * max(int(n), 1))()
+        self.check(self.L.opx_step_measured(self.h, int(n), out))
+        return list(out)[:max(int(n), 0)]
 
     def energy_density(self):
         out = np.empty(self.V)

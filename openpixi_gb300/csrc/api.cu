@@ -3,6 +3,7 @@
 // A handle is one lattice on one GPU with its own CUDA stream: the device
 // counterpart of physics/grid/Grid.java plus the FastTYMSolver selected by
 // physics/Settings.java:540-581, the CGC particle list and the diagnostics.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -80,9 +81,10 @@ static void release(Ctx &c) {
     super_free(c);
     cgc_vt_free(c);
     void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.red_count, c.status,
-                   c.imp_Ua, c.imp_Ub, c.imp_E};
+                   c.imp_Ua, c.imp_Ub, c.imp_E, c.E_alt, c.W_in, c.W_out, c.meas_part, c.meas_rows};
     for (void *p : dev) if (p) cudaFree(p);
     if (c.red_host) cudaFreeHost(c.red_host);
+    if (c.meas_host) cudaFreeHost(c.meas_host);
     if (c.status_host) cudaFreeHost(c.status_host);
     if (c.ev0) cudaEventDestroy(c.ev0);
     if (c.ev1) cudaEventDestroy(c.ev1);
@@ -449,28 +451,13 @@ int opx_synchronize(opx_ctx *ctx) {
 
 long opx_steps_done(const opx_ctx *ctx) { return ctx ? ctx->c.steps : -1; }
 
-int opx_reduce(opx_ctx *ctx, opx_observables *out) {
-    API_CHECK_RO(ctx);
-    Ctx &c = ctx->c;
-    if (!out) { c.err = "opx_reduce: null output"; return OPX_ERR_INVALID; }
-    // the only call since the last reduction that could change the fields was
-    // opx_step(ctx, 1): U now is the Unext that reduction summed B^2 over
-    const bool reuse = c.bcache.calls >= 0 && c.api_calls == c.bcache.calls + 1 && c.step1_call == c.api_calls &&
-                       c.steps == c.bcache.steps + 1 && c.U == c.bcache.unext;
-    c.bcache.calls = -1;
-    phase_begin(c);
-    launch_bulk(c, reuse ? 1 : 0);
-    cudaMemcpyAsync(c.red_host, c.red_out, sizeof(double) * BULK_COLUMNS, cudaMemcpyDeviceToHost, c.stream);
-    int rc = sync_check(c, "opx_reduce");
-    phase_end(c, OPX_PHASE_DIA);
-    if (rc) return rc;
+// BulkQuantitiesInTime's row from the column sums r (the layout of
+// c.red_out) with B^2 of U taken from bu (BulkQuantitiesInTime.java:83-121)
+static int fill_observables(Ctx &c, const double *r, const double *bu, const char *where, opx_observables *out) {
     const double V = (double)c.L.V;
-    const double *r = c.red_host;
-    double bu[3];
-    for (int i = 0; i < 3; i++) bu[i] = reuse ? c.bcache.bn[i] : r[3 + i];
     for (int q = 0; q < BULK_COLUMNS; q++)
         if (!std::isfinite(q >= 3 && q < 6 ? bu[q - 3] : r[q])) {
-            c.err = "opx_reduce: non-finite field values (NaN/Inf) on the lattice";
+            c.err = std::string(where) + ": non-finite field values (NaN/Inf) on the lattice";
             return OPX_ERR_NUMERIC;
         }
     double es[3], bs[3];
@@ -487,10 +474,133 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out) {
     out->rho2 = std::sqrt(r[7]) / V;
     out->e2_total = es[0] + es[1] + es[2];
     out->b2_total = bs[0] + bs[1] + bs[2];
+    return OPX_OK;
+}
+
+int opx_reduce(opx_ctx *ctx, opx_observables *out) {
+    API_CHECK_RO(ctx);
+    Ctx &c = ctx->c;
+    if (!out) { c.err = "opx_reduce: null output"; return OPX_ERR_INVALID; }
+    // the only call since the last reduction that could change the fields was
+    // opx_step(ctx, 1): U now is the Unext that reduction summed B^2 over
+    const bool reuse = c.bcache.calls >= 0 && c.api_calls == c.bcache.calls + 1 && c.step1_call == c.api_calls &&
+                       c.steps == c.bcache.steps + 1 && c.U == c.bcache.unext;
+    c.bcache.calls = -1;
+    phase_begin(c);
+    launch_bulk(c, reuse ? 1 : 0);
+    cudaMemcpyAsync(c.red_host, c.red_out, sizeof(double) * BULK_COLUMNS, cudaMemcpyDeviceToHost, c.stream);
+    int rc = sync_check(c, "opx_reduce");
+    phase_end(c, OPX_PHASE_DIA);
+    if (rc) return rc;
+    const double *r = c.red_host;
+    double bu[3];
+    for (int i = 0; i < 3; i++) bu[i] = reuse ? c.bcache.bn[i] : r[3 + i];
+    rc = fill_observables(c, r, bu, "opx_reduce", out);
+    if (rc) return rc;
     c.bcache.calls = c.api_calls;
     c.bcache.steps = c.steps;
     c.bcache.unext = c.Unext;
     for (int i = 0; i < 3; i++) c.bcache.bn[i] = r[8 + i];
+    return OPX_OK;
+}
+
+static int ensure_measure_buffers(Ctx &c, int nsteps) {
+    const size_t nE = (size_t)c.L.V * 3 * c.na;
+    bool ok = true;
+    if (!c.E_alt) ok = cudaMalloc(&c.E_alt, nE * c.rsize) == cudaSuccess;
+    for (void **w : {&c.W_in, &c.W_out})
+        if (ok && !*w) {
+            ok = cudaMalloc(w, nE * c.rsize) == cudaSuccess;
+            if (ok) cudaMemsetAsync(*w, 0, nE * c.rsize, c.stream);  // the first step's Gauss term is unused
+        }
+    if (ok && !c.meas_part) {
+        // the partials of up to 64 steps (at most 64 MB): their rows are formed
+        // with one launch per chunk of steps
+        const size_t per_step = sizeof(double) * MEAS_ROW * measured_blocks(c);
+        c.meas_chunk = (int)std::max<size_t>(1, std::min<size_t>(64, ((size_t)64 << 20) / per_step));
+        ok = cudaMalloc((void **)&c.meas_part, per_step * c.meas_chunk) == cudaSuccess;
+        if (!ok) c.meas_chunk = 0;
+    }
+    if (ok && c.meas_rows_cap < nsteps) {
+        if (c.meas_rows) cudaFree(c.meas_rows);
+        if (c.meas_host) cudaFreeHost(c.meas_host);
+        c.meas_rows = c.meas_host = nullptr;
+        c.meas_rows_cap = 0;
+        ok = cudaMalloc((void **)&c.meas_rows, sizeof(double) * 8 * nsteps) == cudaSuccess &&
+             cudaMallocHost((void **)&c.meas_host, sizeof(double) * 8 * nsteps) == cudaSuccess;
+        if (ok) c.meas_rows_cap = nsteps;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        c.err = "opx_step_measured: out of device memory";
+        return OPX_ERR_NOMEM;
+    }
+    return OPX_OK;
+}
+
+int opx_step_measured(opx_ctx *ctx, int nsteps, opx_observables *out) {
+    API_CHECK(ctx);
+    Ctx &c = ctx->c;
+    if (nsteps < 0 || (nsteps > 0 && !out)) { c.err = "opx_step_measured: nsteps < 0 or null output"; return OPX_ERR_INVALID; }
+    if (nsteps == 0) return OPX_OK;
+    if (nsteps == 1 || !measured_step_fusable(c)) {
+        for (int k = 0; k < nsteps; k++) {
+            int rc = opx_step(ctx, 1);
+            if (!rc) rc = opx_reduce(ctx, &out[k]);
+            if (rc) return rc;
+        }
+        return OPX_OK;
+    }
+    int rc = ensure_measure_buffers(c, nsteps);
+    if (rc) return rc;
+    c.bcache.calls = -1;
+    const size_t per_step = (size_t)MEAS_ROW * measured_blocks(c);
+    for (int k0 = 0; k0 < nsteps; k0 += c.meas_chunk) {
+        const int nk = std::min(c.meas_chunk, nsteps - k0);
+        phase_begin(c);
+        for (int k = 0; k < nk; k++) {
+            c.steps++;
+            std::swap(c.U, c.Unext);  // storeFields
+            const bool reunit = c.cfg.reunit_every > 0 && (c.steps % c.cfg.reunit_every) == 0;
+            launch_update_measure(c, reunit, c.E_alt, c.W_in, c.W_out, c.meas_part + per_step * k);
+            std::swap(c.E, c.E_alt);
+            std::swap(c.W_in, c.W_out);
+        }
+        launch_measure_combine(c, c.meas_part, nk, c.meas_rows + 8 * k0);
+        phase_end(c, OPX_PHASE_EOM);
+        // the chunk's rows to the host
+        cudaMemcpyAsync(c.meas_host + 8 * k0, c.meas_rows + 8 * k0, sizeof(double) * 8 * nk, cudaMemcpyDeviceToHost,
+                        c.stream);
+    }
+    // the last state: B^2 of its next links, its Gauss law and rho^2
+    phase_begin(c);
+    launch_bulk(c, 1);
+    cudaMemcpyAsync(c.red_host, c.red_out, sizeof(double) * BULK_COLUMNS, cudaMemcpyDeviceToHost, c.stream);
+    rc = sync_check(c, "opx_step_measured");
+    phase_end(c, OPX_PHASE_DIA);
+    if (rc) return rc;
+    const double *red = c.red_host;
+    for (int k = 0; k < nsteps; k++) {
+        // step k's kernel: E^2 and B^2 of its input links (this state's U);
+        // step k + 1's kernel (or the last reduction): B^2 of Unext and the Gauss law
+        const double *m = c.meas_host + 8 * k, *mn = k + 1 < nsteps ? c.meas_host + 8 * (k + 1) : nullptr;
+        double r[BULK_COLUMNS], bu[3];
+        for (int i = 0; i < 3; i++) {
+            r[i] = m[i];
+            r[3 + i] = 0.0;
+            bu[i] = m[3 + i];
+            r[8 + i] = mn ? mn[3 + i] : red[8 + i];
+        }
+        r[6] = mn ? mn[6] : red[6];
+        r[7] = red[7];
+        rc = fill_observables(c, r, bu, "opx_step_measured", &out[k]);
+        if (rc) return rc;
+    }
+    // a following opx_step(ctx, 1) + opx_reduce may reuse B^2 of Unext
+    c.bcache.calls = c.api_calls;
+    c.bcache.steps = c.steps;
+    c.bcache.unext = c.Unext;
+    for (int i = 0; i < 3; i++) c.bcache.bn[i] = red[8 + i];
     return OPX_OK;
 }
 

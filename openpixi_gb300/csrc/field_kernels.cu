@@ -55,6 +55,106 @@ k_update_grid_su3f_pair(const float *__restrict__ U, float *__restrict__ E, cons
     update_site_pair<I, HAS_J, REUNIT>(U, E, J, Unext, L, sa, sb, va, vb);
 }
 
+// The measured step: the update above plus the per-site BulkQuantities terms
+// it can form from what it loads (update_site_pair with MEAS) and the Gauss
+// law of the previous state from the previous step's transported terms Win
+// (gauss_w_pair); it stores its own in Wout.  Every thread reaches the block
+// reduction, so no thread returns early.  Block partials: FP32 warp sums,
+// combined per block in FP64 and in a fixed order; part[block][MEAS_COLS].
+template <typename I, bool REUNIT>
+__global__ void __launch_bounds__(MEAS_THREADS, 3)
+k_update_measure_su3f_pair(const float *__restrict__ U, float *__restrict__ E, float *__restrict__ Eout,
+                           const float *__restrict__ Win, float *__restrict__ Wout, const float *__restrict__ rho,
+                           float *__restrict__ Unext, Lat L, double *__restrict__ part) {
+    __shared__ float slots[MEAS_COLS * MEAS_THREADS];
+    __shared__ double warp_sums[MEAS_COLS][MEAS_THREADS / 32];
+    float *slot = slots + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < MEAS_COLS; q++) slot[q * MEAS_THREADS] = 0.f;
+    const I t = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+    const I sa = ((t >> 5) << 6) + (t & 31);
+    if (sa < (I)L.V) {
+        I sb = sa + 32;
+        const bool vb = sb < (I)L.V;
+        if (!vb) sb = sa;
+        slot[6 * MEAS_THREADS] = pr::lanes(gauss_w_pair<I>(E, Win, rho, L, sa, sb), true, vb);
+        update_site_pair<I, false, REUNIT, true>(U, E, nullptr, Unext, L, sa, sb, true, vb, Eout, slot, Wout);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < MEAS_COLS; q++) {
+        float v = slot[q * MEAS_THREADS];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) warp_sums[q][w] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < MEAS_COLS) {
+        double v = 0.0;
+#pragma unroll
+        for (int k = 0; k < MEAS_THREADS / 32; k++) v += warp_sums[threadIdx.x][k];
+        part[(long)blockIdx.x * MEAS_COLS + threadIdx.x] = v;
+    }
+}
+
+// Column sums of the block partials in a fixed order (block (q, k): column q
+// of step k of the chunk), with the unit factors of the BulkQuantities
+// columns: (g a_i)^-2 for E^2, (g a_i)^-2 / 2 for B^2 (the U / Unext
+// average).  part[k][nparts][MEAS_COLS] -> rows[k][8].
+__global__ void __launch_bounds__(256) k_measure_combine(const double *__restrict__ part, int nparts, Lat L,
+                                                         double *__restrict__ rows) {
+    __shared__ double ws[8];
+    const int q = blockIdx.x;
+    const double *pk = part + (long)blockIdx.y * nparts * MEAS_COLS;
+    double *row = rows + 8 * blockIdx.y;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += pk[(long)b * MEAS_COLS + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += ws[k];
+        if (q < 6) {
+            const int i = q % 3;
+            const double uf = 1.0 / ((L.g * L.a[i]) * (L.g * L.a[i]));
+            s *= q < 3 ? uf : 0.5 * uf;
+        }
+        row[q] = s;
+    }
+}
+
+bool measured_step_fusable(const Ctx &c) {
+    return c.nc == 3 && c.prec == OPX_F32 && c.pair_kernel && !c.imp_solver && !c.j_nonzero && !c.active &&
+           !c.eval && c.P.n == 0 && c.sg.empty();
+}
+
+int measured_blocks(const Ctx &c) { return grid_for(((c.L.V + 63) / 64) * 32, MEAS_THREADS); }
+
+// One measured step, block partials into part[measured_blocks][MEAS_COLS]:
+// reads c.U, c.E and Win, writes c.Unext, Eout and Wout (the caller swaps Eout
+// into c.E and Wout into Win).
+void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, void *Wout, double *part) {
+    const int nb = measured_blocks(c);
+    const float *U = (const float *)c.U, *rho = (const float *)c.rho, *Wi = (const float *)Win;
+    float *E = (float *)c.E, *Eo = (float *)Eout, *Un = (float *)c.Unext, *Wo = (float *)Wout;
+    if (c.int_offsets) {
+        if (reunit) k_update_measure_su3f_pair<int, true><<<nb, MEAS_THREADS, 0, c.stream>>>(U, E, Eo, Wi, Wo, rho, Un, c.L, part);
+        else k_update_measure_su3f_pair<int, false><<<nb, MEAS_THREADS, 0, c.stream>>>(U, E, Eo, Wi, Wo, rho, Un, c.L, part);
+    } else {
+        if (reunit) k_update_measure_su3f_pair<long, true><<<nb, MEAS_THREADS, 0, c.stream>>>(U, E, Eo, Wi, Wo, rho, Un, c.L, part);
+        else k_update_measure_su3f_pair<long, false><<<nb, MEAS_THREADS, 0, c.stream>>>(U, E, Eo, Wi, Wo, rho, Un, c.L, part);
+    }
+    c.launches += 1;
+}
+
+// The rows of nsteps measured steps from their consecutive partials.
+void launch_measure_combine(Ctx &c, const double *part, int nsteps, double *rows) {
+    k_measure_combine<<<dim3(MEAS_COLS, nsteps), 256, 0, c.stream>>>(part, measured_blocks(c), c.L, rows);
+    c.launches += 1;
+}
+
 // ---------------------------------------------------------------- implicit solver
 // ImplicitTYMSolver (physics/fields/ImplicitTYMSolver.java), SU(2).  The
 // implicit grid is a copy: Ui its links (the latest estimate after its

@@ -103,6 +103,12 @@ struct Ctx {
     // opx_cgc_mv / opx_cgc_mv_super call ([n1 n2][ng], reference layout)
     std::vector<double *> cgc_vt;
     int sg_ppc = 0;
+    // opx_step_measured: the second E buffer (the measured step writes the new
+    // E there and the pointers swap), the transported Gauss-law terms of the
+    // last and the next step, the block partials and the per-step rows
+    void *E_alt = nullptr, *W_in = nullptr, *W_out = nullptr;
+    double *meas_part = nullptr, *meas_rows = nullptr, *meas_host = nullptr;  // rows: device and pinned
+    int meas_rows_cap = 0, meas_chunk = 0;  // steps whose partials meas_part holds
     bool profiling = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double phase_ms[OPX_NUM_PHASES] = {0, 0, 0, 0};
@@ -115,6 +121,15 @@ void launch_update_grid(Ctx &c, bool reunit);
 int launch_implicit_update(Ctx &c);  // ImplicitTYMSolver.step in place of launch_update_grid
 void launch_update_links(Ctx &c);
 void launch_reunit(Ctx &c, void *links);
+// the measured step (SU(3) FP32 paired form, FastTYMSolver, no current, no
+// masks, no particles): row[0..6] = E^2 of the new E [3] (x (g a_i)^-2),
+// B^2 of the step's input links [3] (x (g a_i)^-2 / 2), G^2 of the state
+// before the step (from the previous step's transported terms)
+constexpr int MEAS_ROW = 7;
+bool measured_step_fusable(const Ctx &c);
+int measured_blocks(const Ctx &c);
+void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, void *Wout, double *part);
+void launch_measure_combine(Ctx &c, const double *part, int nsteps, double *rows);  // rows[nsteps][8]
 // ---- reductions (reduce_kernels.cu) ----
 // result in c.red_out[0..10]: E^2[3], B^2 of U [3] (zero with skip_u), G^2, rho^2, B^2 of Unext [3]
 constexpr int BULK_COLUMNS = 11;

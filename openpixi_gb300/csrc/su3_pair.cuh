@@ -37,6 +37,8 @@ __device__ __forceinline__ P neg2(P a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ P sub2(P a, P b) { return __fadd2_rn(a, neg2(b)); }
 __device__ __forceinline__ P zero2() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ float maxl(P a) { return fmaxf(a.x, a.y); }
+// the sum of the lanes whose site counts
+__device__ __forceinline__ float lanes(P a, bool va, bool vb) { return (va ? a.x : 0.f) + (vb ? a.y : 0.f); }
 
 struct M {
     P r[9], i[9];
@@ -426,14 +428,33 @@ template <typename I> __device__ __forceinline__ void coords(const Lat &L, I s, 
 
 }  // namespace pr
 
+// Per-thread measurement columns of the measured step (MEAS below), FP32
+// slots in shared memory, column q of thread t at slot[q * MEAS_THREADS]:
+// E^2 of the new E per direction, |B_d|^2 of the step's input links per
+// direction, the Gauss-law square of the previous state.
+constexpr int MEAS_THREADS = 128;
+constexpr int MEAS_COLS = 7;
+
 // FastTYMSolver.CombinedUpdate for SU(3) FP32 at sites sa and sb; a lane
 // whose flag (va, vb) is false computes but stores nothing (a site past the end
 // of the lattice or an inactive cell).  Same equations and staple order as
 // update_site in leapfrog.cuh.
-template <typename I, bool HAS_J, bool REUNIT>
+//
+// MEAS: the step also measures (FieldMeasurements, the per-site terms of the
+// BulkQuantities pass).  The new E goes to Eout (E is only read), E^2 of the
+// new E is added to slot columns 0-2, and the squared magnetic field of each
+// plane is formed from the forward staple that the update computes anyway:
+// U_i(x) (U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger) is the plaquette P_ij(x) of
+// Grid.getPlaquette for i < j, so |proj(P_ij) a_d/(a_i a_j)|^2 with d the third
+// direction goes to column 3 + d.  For the Gauss law of the new state the step
+// stores W_i(x) = U_i(x)^dagger E_i(x) U_i(x) (its input link, the new E) in
+// Wout: the transported term that the next step reads at x + i.
+template <typename I, bool HAS_J, bool REUNIT, bool MEAS = false>
 __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, float *__restrict__ E,
                                                  const float *__restrict__ J, float *__restrict__ Unext,
-                                                 const Lat &L, I sa, I sb, bool va, bool vb) {
+                                                 const Lat &L, I sa, I sb, bool va, bool vb,
+                                                 float *__restrict__ Eout = nullptr, float *slot = nullptr,
+                                                 float *__restrict__ Wout = nullptr) {
     using namespace pr;
     const I V = (I)L.V, nblk = (I)((L.V + 31) >> 5);
     int xa[3], xb[3];
@@ -455,7 +476,22 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
                 // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
                 const I pja = sa + Da.f(j), pjb = sb + Db.f(j);
                 const M T = mul_adj(load<I>(U, nblk, j, pia, pib), load<I>(U, nblk, i, pja, pjb));
-                acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
+                if constexpr (MEAS) {
+                    const M c = mul_adj(T, load<I>(U, nblk, j, sa, sb));
+                    maxpy(S, f, c);
+                    if (i + jj < 3) {  // i < j: the plane's plaquette, once per site
+                        P b[8];
+                        proj_mul(load<I>(U, nblk, i, sa, sb), c, b);
+                        const int d = 3 - i - j;
+                        const P bf = bc(LatR<float>::bfac(L, d));
+                        P b2 = zero2();
+#pragma unroll
+                        for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); b2 = fma2(b[a], b[a], b2); }
+                        slot[(3 + d) * MEAS_THREADS] += lanes(b2, va, vb);
+                    }
+                } else {
+                    acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
+                }
             }
             {
                 // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
@@ -479,7 +515,24 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
 #pragma unroll
             for (int a = 0; a < 8; a++) e[a] = fma2(pp(__ldg(ja + (I)a * V), __ldg(jb + (I)a * V)), jf, e[a]);
         }
-        float *wa = E + eo + sa, *wb = E + eo + sb;
+        float *wa = (MEAS ? Eout : E) + eo + sa, *wb = (MEAS ? Eout : E) + eo + sb;
+        if constexpr (MEAS) {
+            P e2 = mul2(e[0], e[0]);
+#pragma unroll
+            for (int a = 1; a < 8; a++) e2 = fma2(e[a], e[a], e2);
+            slot[i * MEAS_THREADS] += lanes(e2, va, vb);
+            P w[8];
+            herm_gen(mul(adj_mul(Ui, herm(e)), Ui), w);
+            float *xa = Wout + eo + sa, *xb = Wout + eo + sb;
+            if (va) {
+#pragma unroll
+                for (int a = 0; a < 8; a++) xa[(I)a * V] = w[a].x;
+            }
+            if (vb) {
+#pragma unroll
+                for (int a = 0; a < 8; a++) xb[(I)a * V] = w[a].y;
+            }
+        }
         if (va) {
 #pragma unroll
             for (int a = 0; a < 8; a++) wa[(I)a * V] = e[a].x;
@@ -495,6 +548,42 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
         if (REUNIT) reunit(Vn);
         store<I>(Unext, nblk, i, sa, sb, va, vb, Vn);
     }
+}
+
+// Gauss-law square of the state before a step (Grid.getGaussConstraintSquared,
+// Grid.java:944-968):
+//   G(x) = sum_i [E_i(x) - W_i(x-i)] gfac_i - rho(x),  W_i(y) = U_i(y)^dagger E_i(y) U_i(y)
+// with E the step's input E and W the previous step's transported terms.
+template <typename I>
+__device__ __forceinline__ pr::P gauss_w_pair(const float *__restrict__ E, const float *__restrict__ W,
+                                              const float *__restrict__ rho, const Lat &L, I sa, I sb) {
+    using namespace pr;
+    const I V = (I)L.V;
+    int xa[3], xb[3];
+    coords<I>(L, sa, xa);
+    coords<I>(L, sb, xb);
+    const Deltas<I> Da = deltas<I>(L, xa), Db = deltas<I>(L, xb);
+    P gs[8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) gs[a] = zero2();
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const I mia = sa + Da.b(i), mib = sb + Db.b(i);
+        const I eo = (I)i * 8 * V;
+        const P gf = bc(LatR<float>::gfac(L, i));
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            const P e0 = pp(__ldg(E + eo + (I)a * V + sa), __ldg(E + eo + (I)a * V + sb));
+            const P w = pp(__ldg(W + eo + (I)a * V + mia), __ldg(W + eo + (I)a * V + mib));
+            gs[a] = fma2(sub2(e0, w), gf, gs[a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 8; a++) gs[a] = sub2(gs[a], pp(__ldg(rho + (I)a * V + sa), __ldg(rho + (I)a * V + sb)));
+    P g2 = mul2(gs[0], gs[0]);
+#pragma unroll
+    for (int a = 1; a < 8; a++) g2 = fma2(gs[a], gs[a], g2);
+    return g2;
 }
 
 }  // namespace opx

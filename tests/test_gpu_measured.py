@@ -1,0 +1,129 @@
+"""opx_step_measured: n steps with the BulkQuantities row after each.
+
+For SU(3) FP32 handles (FastTYMSolver, no current, masks or particles) each
+step's kernel forms the per-site terms it can from what it loads (E^2 of the
+new E, B^2 of its input links, the Gauss law of the state before it) and one
+reduction follows the last step.  A twin handle on the same initial fields runs
+opx_step(ctx, 1) + opx_reduce per step:
+  - the fields after the run are bit-identical (the same update arithmetic);
+  - the rows agree to FP32 rounding of the per-site terms (written tolerances);
+  - a following step + reduce is bit-identical on both (the B^2 reuse holds).
+Every other configuration, and nsteps = 1, is step + reduce itself: bit-identical.
+"""
+import numpy as np
+import pytest
+
+import openpixi_gb300 as opx
+from openpixi_gb300 import _native as N
+from tests.helpers import oracle_ic, fresh
+
+pytestmark = pytest.mark.gpu
+
+
+def vec(o):
+    return np.array(list(o.e2) + list(o.b2) + [o.px, o.py, o.pz, o.gauss, o.rho2, o.e2_total, o.b2_total])
+
+
+def twins(nc, dims, prec, reunit, seed=31, sigma=0.3, rho=False, kick=0.0):
+    """Two handles on the same initial fields.  The oracle's initial E satisfies
+    the Gauss law; kick adds Gaussian noise of that width to E (generator
+    components) so that the Gauss-law term is far from zero."""
+    g = fresh(oracle_ic(nc, dims, seed, sigma, sigma))
+    hs = []
+    e_kicked = None
+    for _ in range(2):
+        h = opx.Handle(nc, dims, a=g.a, dt=g.dt, g=g.g, precision=prec, reunit_every=reunit)
+        h.upload(N.FIELD_U, g.U)
+        h.upload(N.FIELD_E, g.E)
+        if kick:
+            if e_kicked is None:
+                e = h.download(N.FIELD_E, layout=N.LAYOUT_GEN)
+                e_kicked = e + np.random.default_rng(seed + 1).normal(0.0, kick, size=e.shape)
+            h.upload(N.FIELD_E, e_kicked, layout=N.LAYOUT_GEN)
+        if rho:
+            r = np.random.default_rng(seed).normal(0.0, 0.05, size=h.V * h.ngen)
+            h.upload(N.FIELD_RHO, r, layout=N.LAYOUT_GEN)
+        h.initialize()
+        hs.append(h)
+    return hs
+
+
+def loop(h, n):
+    out = []
+    for _ in range(n):
+        h.step(1)
+        out.append(h.reduce())
+    return out
+
+
+# FP32 rounding of the per-site terms: E^2 terms are identical per site (only the
+# summation order differs), B^2 terms are products in another association, the
+# Gauss-law terms are formed in another kernel (the same operations)
+RTOL_E2 = 1e-6
+RTOL_B2 = 3e-6
+RTOL_GAUSS = 1e-5
+
+
+@pytest.mark.parametrize("dims,reunit,rho,kick", [
+    ((16, 16, 16), 4, False, 0.05),   # reunitarisation steps inside the run
+    ((12, 10, 14), 0, True, 0.0),     # V = 1680: the last thread has one site; a static charge density
+    ((24, 20, 16), 3, False, 0.05),
+])
+def test_fused_rows_match_step_and_reduce(native, dims, reunit, rho, kick):
+    a, b = twins(3, dims, N.OPX_F32, reunit, rho=rho, kick=kick)
+    a.reduce(), b.reduce()
+    n = 9
+    ra = a.step_measured(n)
+    rb = loop(b, n)
+    assert a.steps_done == b.steps_done
+    for f in (N.FIELD_U, N.FIELD_UNEXT, N.FIELD_E):
+        assert np.array_equal(a.download(f), b.download(f)), f
+    for oa, ob in zip(ra, rb):
+        va, vb = vec(oa), vec(ob)
+        scale = ob.e2_total + ob.b2_total
+        np.testing.assert_allclose(va[0:3], vb[0:3], rtol=RTOL_E2, atol=0)
+        np.testing.assert_allclose(va[3:6], vb[3:6], rtol=RTOL_B2, atol=0)
+        np.testing.assert_allclose(va[6:9], vb[6:9], rtol=0, atol=RTOL_B2 * scale)
+        np.testing.assert_allclose(va[9], vb[9], rtol=RTOL_GAUSS, atol=1e-9 * scale)
+        assert va[10] == vb[10]  # rho^2: the same reduction
+        np.testing.assert_allclose(va[11:], vb[11:], rtol=RTOL_B2, atol=0)
+    # the Gauss law of these fields is far from zero (the kick or the charge
+    # density), so the comparison above tests the Gauss term, not rounding noise
+    assert rb[0].gauss > 1e-4 * (rb[0].e2_total + rb[0].b2_total)
+    # a following step + reduce reuses B^2 and is bit-identical on both handles
+    a.step(1)
+    b.step(1)
+    assert np.array_equal(vec(a.reduce()), vec(b.reduce()))
+
+
+@pytest.mark.parametrize("nc,dims,prec,n", [
+    (3, (8, 8, 8), N.OPX_F64, 5),
+    (2, (10, 8, 12), N.OPX_F32, 5),
+    (3, (12, 12, 12), N.OPX_F32, 1),   # one step: step + reduce
+])
+def test_other_forms_are_step_and_reduce(native, nc, dims, prec, n):
+    a, b = twins(nc, dims, prec, 0)
+    a.reduce(), b.reduce()
+    ra = a.step_measured(n)
+    rb = loop(b, n)
+    for oa, ob in zip(ra, rb):
+        assert np.array_equal(vec(oa), vec(ob))
+    assert np.array_equal(a.download(N.FIELD_E), b.download(N.FIELD_E))
+
+
+def test_masks_take_the_plain_path(native):
+    a, b = twins(3, (12, 12, 12), N.OPX_F32, 0)
+    ones = np.ones(a.V, dtype=np.uint8)
+    a.set_evaluatable(ones)
+    b.set_evaluatable(ones)
+    ra = a.step_measured(4)
+    rb = loop(b, 4)
+    for oa, ob in zip(ra, rb):
+        assert np.array_equal(vec(oa), vec(ob))
+
+
+def test_invalid_arguments(native):
+    a, _ = twins(3, (8, 8, 8), N.OPX_F32, 0)
+    assert a.step_measured(0) == []
+    with pytest.raises(opx.OpixiError):
+        a.step_measured(-1)
