@@ -711,7 +711,8 @@ def main():
             h2.initialize()
             t_in = time.perf_counter()
             if measured:
-                rows = h2.step_measured(args.steps)
+                with nvtx_range("e2e_measured"):
+                    rows = h2.step_measured(args.steps)
             else:
                 rows = []
                 for k in range(args.steps):
