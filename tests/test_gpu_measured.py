@@ -127,3 +127,30 @@ def test_invalid_arguments(native):
     assert a.step_measured(0) == []
     with pytest.raises(opx.OpixiError):
         a.step_measured(-1)
+
+
+def test_long_offsets_match(native, monkeypatch):
+    """The measured step with 64-bit offsets (OPX_LONG_OFFSETS=1 at handle
+    creation) against the 32-bit form: bit-identical fields and rows."""
+    a, _ = twins(3, (12, 10, 14), N.OPX_F32, 4, kick=0.05)
+    monkeypatch.setenv("OPX_LONG_OFFSETS", "1")
+    b, _ = twins(3, (12, 10, 14), N.OPX_F32, 4, kick=0.05)
+    monkeypatch.delenv("OPX_LONG_OFFSETS")
+    ra, rb = a.step_measured(7), b.step_measured(7)
+    for f in (N.FIELD_U, N.FIELD_UNEXT, N.FIELD_E):
+        assert np.array_equal(a.download(f), b.download(f)), f
+    for oa, ob in zip(ra, rb):
+        assert np.array_equal(vec(oa), vec(ob))
+
+
+def test_repeated_calls_continue_the_run(native):
+    """Two calls of 4 and 5 steps give the rows of one call of 9 (the second
+    call's first row takes its Gauss law and B^2 of Unext from its own kernels)."""
+    a, b = twins(3, (16, 12, 10), N.OPX_F32, 3, kick=0.05)
+    ra = a.step_measured(4) + a.step_measured(5)
+    rb = b.step_measured(9)
+    for f in (N.FIELD_U, N.FIELD_E):
+        assert np.array_equal(a.download(f), b.download(f)), f
+    for oa, ob in zip(ra, rb):
+        va, vb = vec(oa), vec(ob)
+        np.testing.assert_allclose(va, vb, rtol=RTOL_GAUSS, atol=RTOL_B2 * (ob.e2_total + ob.b2_total))
