@@ -443,10 +443,10 @@ constexpr int MEAS_COLS = 7;
 // MEAS: the step also measures (FieldMeasurements, the per-site terms of the
 // BulkQuantities pass).  The new E goes to Eout (E is only read), E^2 of the
 // new E is added to slot columns 0-2, and the squared magnetic field of each
-// plane is formed from the forward staple that the update computes anyway:
-// U_i(x) (U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger) is the plaquette P_ij(x) of
-// Grid.getPlaquette for i < j, so |proj(P_ij) a_d/(a_i a_j)|^2 with d the third
-// direction goes to column 3 + d.  For the Gauss law of the new state the step
+// plane is formed from a forward staple that the update computes anyway:
+// U_i(x) (U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger) with j = i + 1 is the
+// plaquette P_ij(x) of Grid.getPlaquette, so |proj(P_ij) a_d/(a_i a_j)|^2 with
+// d = i + 2 goes to column 3 + d (one plane per link, each plane once).  For the Gauss law of the new state the step
 // stores W_i(x) = U_i(x)^dagger E_i(x) U_i(x) (its input link, the new E) in
 // Wout: the transported term that the next step reads at x + i.
 template <typename I, bool HAS_J, bool REUNIT, bool MEAS = false>
@@ -466,33 +466,16 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
     for (int i = 0; i < 3; i++) {
         const I pia = sa + Da.f(i), pib = sb + Db.f(i);  // x + i
         M S = mzero();
+        [[maybe_unused]] M Pl;  // MEAS: the forward staple of plane i + 1
         // the two staple planes unrolled: their loads and products interleave
-        // (1 % faster than the rolled loop at 128^3, same registers)
+        // (1 % faster than the rolled loop at 128^3, same registers).  Plane
+        // i + 2 before plane i + 1, each backward staple before the forward
+        // one, so that the last staple formed is the forward staple of plane
+        // i + 1, whose product with U_i(x) is the plaquette P_{i,i+1}(x).
 #pragma unroll
-        for (int jj = 1; jj < 3; jj++) {
+        for (int jj = 2; jj >= 1; jj--) {
             const int j = i + jj >= 3 ? i + jj - 3 : i + jj;
             const P f = bc(LatR<float>::inva2(L, j));
-            {
-                // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
-                const I pja = sa + Da.f(j), pjb = sb + Db.f(j);
-                const M T = mul_adj(load<I>(U, nblk, j, pia, pib), load<I>(U, nblk, i, pja, pjb));
-                if constexpr (MEAS) {
-                    const M c = mul_adj(T, load<I>(U, nblk, j, sa, sb));
-                    maxpy(S, f, c);
-                    if (i + jj < 3) {  // i < j: the plane's plaquette, once per site
-                        P b[8];
-                        proj_mul(load<I>(U, nblk, i, sa, sb), c, b);
-                        const int d = 3 - i - j;
-                        const P bf = bc(LatR<float>::bfac(L, d));
-                        P b2 = zero2();
-#pragma unroll
-                        for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); b2 = fma2(b[a], b[a], b2); }
-                        slot[(3 + d) * MEAS_THREADS] += lanes(b2, va, vb);
-                    }
-                } else {
-                    acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
-                }
-            }
             {
                 // (U_i(x-j) U_j(x+i-j))^dagger U_j(x-j)
                 const I bja = Da.b(j), bjb = Db.b(j);
@@ -501,10 +484,33 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
                 const M C = mul(load<I>(U, nblk, i, mja, mjb), load<I>(U, nblk, j, pimja, pimjb));
                 acc_adj_mul(S, f, C, load<I>(U, nblk, j, mja, mjb));
             }
+            {
+                // U_j(x+i) U_i(x+j)^dagger U_j(x)^dagger
+                const I pja = sa + Da.f(j), pjb = sb + Db.f(j);
+                const M T = mul_adj(load<I>(U, nblk, j, pia, pib), load<I>(U, nblk, i, pja, pjb));
+                if constexpr (MEAS) {
+                    const M c = mul_adj(T, load<I>(U, nblk, j, sa, sb));
+                    maxpy(S, f, c);
+                    if (jj == 1) Pl = c;
+                } else {
+                    acc_mul_adj(S, f, T, load<I>(U, nblk, j, sa, sb));
+                }
+            }
         }
         const M Ui = load<I>(U, nblk, i, sa, sb);
         P p[8], e[8];
         proj_mul(Ui, S, p);
+        if constexpr (MEAS) {
+            // |B_d|^2, d = i + 2: P_{i,i+1}(x) is Grid.getPlaquette of B_d with (d, j, k) cyclic
+            P b[8];
+            proj_mul(Ui, Pl, b);
+            const int d = i == 0 ? 2 : i - 1;
+            const P bf = bc(LatR<float>::bfac(L, d));
+            P b2 = zero2();
+#pragma unroll
+            for (int a = 0; a < 8; a++) { b[a] = mul2(b[a], bf); b2 = fma2(b[a], b[a], b2); }
+            slot[(3 + d) * MEAS_THREADS] += lanes(b2, va, vb);
+        }
         const I eo = (I)i * 8 * V;
         const float *ea = E + eo + sa, *eb = E + eo + sb;
 #pragma unroll
