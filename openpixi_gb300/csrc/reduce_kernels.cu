@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(RED_THREADS, 3)
             else if (i == 1) kadd(1, ev);
             else kadd(2, ev);
             const M Ub = load<I>(U, nblk, i, mia, mib);
-            herm_gen(mul(adj_mul(Ub, herm(e1)), Ub), tv);
+            act_adj_gen(Ub, e1, tv);
             const P gf = bc(LatR<float>::gfac(L, i));
 #pragma unroll
             for (int a = 0; a < 8; a++) gs[a] = fma2(sub2(e0[a], tv[a]), gf, gs[a]);

@@ -356,6 +356,73 @@ __device__ __forceinline__ void herm_gen(const M &h, P *x) {
     x[6] = sub2(h.i[7], h.i[5]);
     x[7] = mul2(sub2(add2(h.r[0], h.r[4]), add2(h.r[8], h.r[8])), bc(0.57735026918962576451f));
 }
+// w = generator components of u^dagger H u, H = x^a lambda_a / 2 (the parallel
+// transport of SU3AlgebraElement.act with g = u^dagger).  Uses the structure:
+// H has a real diagonal, and the result is hermitian, so only its real
+// diagonal and upper triangle are formed.
+__device__ __forceinline__ void act_adj_gen(const M &u, const P *x, P *w) {
+    const P half = bc(0.5f), mhalf = bc(-0.5f), c2s3 = bc(0.28867513459481288225f);
+    P hd[3], hr[3], hi[3];  // diagonal; off-diagonal (0,1), (0,2), (1,2)
+    hd[0] = fma2(half, x[2], mul2(c2s3, x[7]));
+    hd[1] = sub2(mul2(c2s3, x[7]), mul2(half, x[2]));
+    hd[2] = mul2(bc(-0.57735026918962576451f), x[7]);
+    hr[0] = mul2(half, x[0]); hi[0] = mul2(mhalf, x[1]);
+    hr[1] = mul2(half, x[3]); hi[1] = mul2(mhalf, x[4]);
+    hr[2] = mul2(half, x[5]); hi[2] = mul2(mhalf, x[6]);
+    // A = H u
+    M A;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            P re = mul2(hd[r], u.r[3 * r + q]), im = mul2(hd[r], u.i[3 * r + q]);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (k == r) continue;
+                // H_rk: upper entries stored, lower ones their conjugates
+                const int o = (r == 0 || k == 0) ? (r + k - 1) : 2;
+                const P a = hr[o], b = r < k ? hi[o] : neg2(hi[o]);
+                re = fma2(a, u.r[3 * k + q], fma2(neg2(b), u.i[3 * k + q], re));
+                im = fma2(a, u.i[3 * k + q], fma2(b, u.r[3 * k + q], im));
+            }
+            A.r[3 * r + q] = re;
+            A.i[3 * r + q] = im;
+        }
+    // W = u^dagger A: real diagonal and upper triangle
+    P wd[3], wr[3], wi[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        P d = mul2(u.r[r], A.r[r]);
+        d = fma2(u.i[r], A.i[r], d);
+#pragma unroll
+        for (int k = 1; k < 3; k++) { d = fma2(u.r[3 * k + r], A.r[3 * k + r], d); d = fma2(u.i[3 * k + r], A.i[3 * k + r], d); }
+        wd[r] = d;
+    }
+#pragma unroll
+    for (int o = 0; o < 3; o++) {
+        const int r = o == 2 ? 1 : 0, q = o == 0 ? 1 : 2;
+        P re = mul2(u.r[r], A.r[q]), im = mul2(u.r[r], A.i[q]);
+        re = fma2(u.i[r], A.i[q], re);
+        im = fma2(neg2(u.i[r]), A.r[q], im);
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+            re = fma2(u.r[3 * k + r], A.r[3 * k + q], fma2(u.i[3 * k + r], A.i[3 * k + q], re));
+            im = fma2(u.r[3 * k + r], A.i[3 * k + q], fma2(neg2(u.i[3 * k + r]), A.r[3 * k + q], im));
+        }
+        wr[o] = re;
+        wi[o] = im;
+    }
+    const P two = bc(2.f), mtwo = bc(-2.f);
+    w[0] = mul2(two, wr[0]);
+    w[1] = mul2(mtwo, wi[0]);
+    w[2] = sub2(wd[0], wd[1]);
+    w[3] = mul2(two, wr[1]);
+    w[4] = mul2(mtwo, wi[1]);
+    w[5] = mul2(two, wr[2]);
+    w[6] = mul2(mtwo, wi[2]);
+    w[7] = mul2(sub2(add2(wd[0], wd[1]), add2(wd[2], wd[2])), bc(0.57735026918962576451f));
+}
+
 // proj(M) for a whole matrix
 __device__ __forceinline__ void proj(const M &m, P *x) {
     x[0] = add2(m.i[1], m.i[3]);
@@ -528,7 +595,7 @@ __device__ __forceinline__ void update_site_pair(const float *__restrict__ U, fl
             for (int a = 1; a < 8; a++) e2 = fma2(e[a], e[a], e2);
             slot[i * MEAS_THREADS] += lanes(e2, va, vb);
             P w[8];
-            herm_gen(mul(adj_mul(Ui, herm(e)), Ui), w);
+            act_adj_gen(Ui, e, w);
             float *xa = Wout + eo + sa, *xb = Wout + eo + sb;
             if (va) {
 #pragma unroll
