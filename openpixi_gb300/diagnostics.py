@@ -92,7 +92,10 @@ class BulkQuantitiesInTime(Diagnostics):
     def calculate(self, grid, particles, steps):
         if steps % self.stepInterval != 0:
             return
-        o = grid.reduce()
+        self.record(grid.reduce(), steps)
+
+    def record(self, o, steps):
+        """One row from the observables o (opx_observables) at step `steps`."""
         self.eSquared, self.bSquared = o.e2_total, o.b2_total
         self.px, self.py, self.pz = o.px, o.py, o.pz
         self.gaussViolation, self.totalChargeSquared = o.gauss, o.rho2

@@ -302,8 +302,31 @@ class Simulation:
         return self.totalSimulationSteps <= self.iterations
 
     def run(self):
+        """Simulation.run: step while continues().  When BulkQuantitiesInTime at
+        every step is the only diagnostic, the updates after step 0 run as one
+        opx_step_measured call (MainBatch's loop in one call; the same rows)."""
+        if self.continues() and self._measured_loop():
+            if self.totalSimulationSteps == 0:
+                for d in self.diagnostics:
+                    d.initialize(self)
+                self.runDiagnostics()
+            n = self.iterations + 1 - self.totalSimulationSteps
+            rows = self.grid.handle.step_measured(n)
+            self.grid._dirty()
+            for o in rows:
+                self.totalSimulationSteps += 1
+                self.totalSimulationTime = self.totalSimulationSteps * self.tstep
+                self.grid.simulationSteps = self.totalSimulationSteps
+                for d in self.diagnostics:
+                    d.record(o, self.totalSimulationSteps)
         while self.continues():
             self.step()
+
+    def _measured_loop(self):
+        from .diagnostics import BulkQuantitiesInTime
+        if not self.diagnostics or not all(type(d) is BulkQuantitiesInTime for d in self.diagnostics):
+            return False
+        return all(max(round(d.timeInterval / self.tstep), 1) == 1 for d in self.diagnostics)
 
     def runDiagnostics(self):
         for d in self.diagnostics:

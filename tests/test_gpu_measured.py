@@ -154,3 +154,56 @@ def test_repeated_calls_continue_the_run(native):
     for oa, ob in zip(ra, rb):
         va, vb = vec(oa), vec(ob)
         np.testing.assert_allclose(va, vb, rtol=RTOL_GAUSS, atol=RTOL_B2 * (ob.e2_total + ob.b2_total))
+
+
+def test_simulation_run_uses_the_measured_loop(native, tmp_path):
+    """Simulation.run with BulkQuantitiesInTime at every step as the only
+    diagnostic hands the updates to opx_step_measured; its file has the rows of
+    the step-by-step loop (Simulation.step while continues()) to FP32 rounding of
+    the per-site terms, and the same number of rows (step 0 plus iterations + 1
+    updates)."""
+    from openpixi_gb300 import settings as S
+    from openpixi_gb300.simulation import Simulation
+
+    def deck(path):
+        return f"""
+simulationType: temporal yang-mills
+gridStep: 1
+couplingConstant: 1
+numberOfDimensions: 3
+numberOfColors: 3
+gridCells: [12, 10, 16]
+timeStep: 0.05
+duration: 0.5
+initialConditions:
+  randomGaussian:
+    - randomSeed: 11
+      sigmaA: 0.2
+      sigmaE: 0.2
+output:
+  bulkQuantitiesInTime:
+    - path: {path}
+      interval: 0.05
+gpu:
+  precision: f32
+  reunitarizeEvery: 4
+"""
+    fa, fb = tmp_path / "a.txt", tmp_path / "b.txt"
+    a = Simulation(S.settings_from_string(deck(fa)))
+    b = Simulation(S.settings_from_string(deck(fb)))
+    assert a._measured_loop()
+    a.run()
+    while b.continues():
+        b.step()
+    assert a.totalSimulationSteps == b.totalSimulationSteps == b.iterations + 1
+    ra = [[float(v) for v in ln.split("\t")] for ln in fa.read_text().splitlines()[1:]]
+    rb = [[float(v) for v in ln.split("\t")] for ln in fb.read_text().splitlines()[1:]]
+    assert len(ra) == len(rb) == b.iterations + 2
+    for x, y in zip(ra, rb):
+        assert x[0] == y[0]
+        scale = y[1] + y[2]
+        np.testing.assert_allclose(x[1:3], y[1:3], rtol=RTOL_B2)
+        np.testing.assert_allclose(x[3:6], y[3:6], rtol=0, atol=RTOL_B2 * scale)
+        np.testing.assert_allclose(x[6], y[6], rtol=RTOL_GAUSS, atol=1e-9 * scale)
+    for f in (N.FIELD_U, N.FIELD_E):
+        assert np.array_equal(a.grid.handle.download(f), b.grid.handle.download(f))
