@@ -165,7 +165,9 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out);
  * forms) and one reduction follows the last step; the values agree with
  * opx_step + opx_reduce to FP32 rounding of the per-site terms (the plaquettes
  * are multiplied in another order, the sums run in another order).  Otherwise,
- * and for nsteps = 1, it is exactly opx_step(ctx, 1) + opx_reduce per step. */
+ * and for nsteps = 1, it is exactly opx_step(ctx, 1) + opx_reduce per step.
+ * OPX_ERR_NUMERIC (non-finite values): the steps were made, and the rows before
+ * the first non-finite one are filled. */
 int opx_step_measured(opx_ctx *ctx, int nsteps, opx_observables *out);
 /* EnergyDensity.ComponentComputation (diagnostics/methods/EnergyDensity.java:119-166): V doubles */
 int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count);
