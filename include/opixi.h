@@ -166,8 +166,9 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out);
  * opx_step + opx_reduce to FP32 rounding of the per-site terms (the plaquettes
  * are multiplied in another order, the sums run in another order).  Otherwise,
  * and for nsteps = 1, it is exactly opx_step(ctx, 1) + opx_reduce per step.
- * OPX_ERR_NUMERIC (non-finite values): the steps were made, and the rows before
- * the first non-finite one are filled. */
+ * OPX_ERR_NUMERIC (non-finite values): the rows before the first non-finite one
+ * are filled; the fused form has made all nsteps steps, the step + reduce form
+ * stops after the step of that row. */
 int opx_step_measured(opx_ctx *ctx, int nsteps, opx_observables *out);
 /* EnergyDensity.ComponentComputation (diagnostics/methods/EnergyDensity.java:119-166): V doubles */
 int opx_energy_density(opx_ctx *ctx, double *host_out, size_t count);
