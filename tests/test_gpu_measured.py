@@ -207,3 +207,26 @@ gpu:
         np.testing.assert_allclose(x[6], y[6], rtol=RTOL_GAUSS, atol=1e-9 * scale)
     for f in (N.FIELD_U, N.FIELD_E):
         assert np.array_equal(a.grid.handle.download(f), b.grid.handle.download(f))
+
+
+def test_non_finite_fields_are_reported(native):
+    """A NaN in E (planted on the host) ends the call with OPX_ERR_NUMERIC and
+    the handle stays usable."""
+    a, _ = twins(3, (8, 8, 8), N.OPX_F32, 0)
+    e = a.download(N.FIELD_E, layout=N.LAYOUT_GEN)
+    e.reshape(-1)[123] = np.nan
+    a.upload(N.FIELD_E, e, layout=N.LAYOUT_GEN)
+    with pytest.raises(N.OpixiError) as err:
+        a.step_measured(3)
+    assert err.value.code == N.OPX_ERR_NUMERIC
+    a.upload(N.FIELD_E, np.zeros_like(e), layout=N.LAYOUT_GEN)
+    a.upload(N.FIELD_U, identity_links(a))
+    a.initialize()
+    rows = a.step_measured(3)
+    assert all(o.e2_total == 0.0 and o.b2_total == 0.0 for o in rows)
+
+
+def identity_links(h):
+    u = np.zeros((h.V, 3, 18))
+    u[:, :, [0, 4, 8]] = 1.0  # re[0], re[4], re[8] of the row-major re[9], im[9] layout
+    return u
