@@ -281,7 +281,8 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
     {16,24,32,40,48}^3, FP32 with reunitarisation every 10 steps, 200 steps in
     one persistent launch replayed from a CUDA graph (autotuned cluster / block
     size), against the plain FP64 single-lattice path looping over the same
-    events (GPU time of each event's 200 steps, summed)."""
+    events (GPU time of each event's 200 steps, summed), which also gives the
+    batch's energy error after 200 steps (max over the events)."""
     import openpixi_gb300 as opx
     from openpixi_gb300 import _native as N
     rng = np.random.default_rng(seed)
@@ -290,25 +291,32 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
     b = opx.Batch(2, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
     b.init_random([seed + 1000 + q for q in range(nev)], 0.1, 0.1, tol=1e-24)
     b.initialize()
-    cluster, block = b.autotune(steps=5)
+    init = [(b.download(q, N.FIELD_U), b.download(q, N.FIELD_E)) for q in range(nev)]
+    cluster, block = b.autotune(steps=5)  # restores the fields
     b.run(nsteps)  # instantiates the graph
+    obs_first = b.reduce()  # the events after their first nsteps steps
     b.run(nsteps)
     l0 = b.kernel_launches
     ms = b.time_run(nsteps)
     launches = b.kernel_launches - l0
     links = 3 * sum(L ** 3 for L in sizes)
     obs = b.reduce()
-    # plain FP64 path, one lattice at a time, same fields
+    # plain FP64 path, one lattice at a time, from the same initial fields: its
+    # time, and the FP32 batch's energy error after nsteps steps against it
     handles = {}
     ms64 = 0.0
+    derr = 0.0
     for q, d in enumerate(dims):
         h = handles.get(d)
         if h is None:
             h = handles[d] = opx.Handle(2, d, dt=0.05, precision=N.OPX_F64, device=device)
-        h.upload(N.FIELD_U, b.download(q, N.FIELD_U))
-        h.upload(N.FIELD_E, b.download(q, N.FIELD_E))
+        h.upload(N.FIELD_U, init[q][0])
+        h.upload(N.FIELD_E, init[q][1])
         h.initialize()
         ms64 += h.time_steps(nsteps)
+        o = h.reduce()
+        e64 = o.e2_total + o.b2_total
+        derr = max(derr, abs(obs_first[q].e2_total + obs_first[q].b2_total - e64) / abs(e64))
     for h in handles.values():
         h.close()
     peak, _ = hbm_peak()
@@ -319,7 +327,8 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
             "link_updates_per_s": lu, "roofline_frac": 56.0 * lu / 1e9 / peak, "bytes_per_link": 56,
             "fp64_loop_ms": ms64, "fp64_loop_events_per_s": nev / (ms64 / 1000.0),
             "speedup_vs_fp64_loop": ms64 / ms, "cluster": cluster, "block": block, "graph": True,
-            "gpu_launches": launches, "max_gauss": max(o.gauss for o in obs)}
+            "gpu_launches": launches, "max_gauss": max(o.gauss for o in obs),
+            "energy_rel_err_vs_fp64": derr}
 
 
 CGC_DIMS = (256, 64, 64)
