@@ -81,7 +81,7 @@ static void release(Ctx &c) {
     super_free(c);
     cgc_vt_free(c);
     void *dev[] = {c.U, c.Unext, c.E, c.J, c.rho, c.active, c.eval, c.staging, c.red_part, c.red_out, c.red_count, c.status,
-                   c.imp_Ua, c.imp_Ub, c.imp_E, c.E_alt, c.W_in, c.W_out, c.meas_part, c.meas_rows};
+                   c.imp_Ua, c.imp_Ub, c.imp_E, c.E_alt, c.W_in, c.W_out, c.meas_part, c.meas_rows, c.bn_site};
     for (void *p : dev) if (p) cudaFree(p);
     if (c.red_host) cudaFreeHost(c.red_host);
     if (c.meas_host) cudaFreeHost(c.meas_host);
@@ -486,6 +486,13 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out) {
     const bool reuse = c.bcache.calls >= 0 && c.api_calls == c.bcache.calls + 1 && c.step1_call == c.api_calls &&
                        c.steps == c.bcache.steps + 1 && c.U == c.bcache.unext;
     c.bcache.calls = -1;
+    // the generic pass also leaves the per-site B^2 of Unext for ProjectedEnergyDensity
+    const bool generic = !(c.nc == 3 && c.prec == OPX_F32 && c.pair_kernel);
+    if (generic && !c.bn_site && cudaMalloc((void **)&c.bn_site, sizeof(double) * 3 * c.L.V) != cudaSuccess) {
+        cudaGetLastError();
+        c.bn_site = nullptr;  // no cache: ProjectedEnergyDensity forms the plaquettes
+    }
+    c.bnsite.calls = -1;
     phase_begin(c);
     launch_bulk(c, reuse ? 1 : 0);
     cudaMemcpyAsync(c.red_host, c.red_out, sizeof(double) * BULK_COLUMNS, cudaMemcpyDeviceToHost, c.stream);
@@ -501,6 +508,11 @@ int opx_reduce(opx_ctx *ctx, opx_observables *out) {
     c.bcache.steps = c.steps;
     c.bcache.unext = c.Unext;
     for (int i = 0; i < 3; i++) c.bcache.bn[i] = r[8 + i];
+    if (generic && c.bn_site) {
+        c.bnsite.calls = c.api_calls;
+        c.bnsite.steps = c.steps;
+        c.bnsite.unext = c.Unext;
+    }
     return OPX_OK;
 }
 
@@ -633,9 +645,12 @@ int opx_projected_energy(opx_ctx *ctx, int dir, double *host_out, size_t count) 
     const bool reuse = pc.calls >= 0 && c.api_calls == pc.calls + 1 && c.step1_call == c.api_calls &&
                        c.steps == pc.steps + 1 && c.U == pc.unext;
     pc.calls = -1;
+    // B^2 of Unext per site from the last opx_reduce when nothing changed since
+    const bool sites = c.bn_site && c.bnsite.calls == c.api_calls && c.bnsite.steps == c.steps &&
+                       c.bnsite.unext == c.Unext;
     std::vector<double> rows(6 * (size_t)ns);
     phase_begin(c);
-    launch_projected_energy(c, dir, reuse ? 1 : 0, c.staging);
+    launch_projected_energy(c, dir, reuse ? 1 : 0, sites ? c.bn_site : nullptr, c.staging);
     cudaMemcpyAsync(rows.data(), c.staging, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, c.stream);
     rc = sync_check(c, "opx_projected_energy");
     phase_end(c, OPX_PHASE_DIA);

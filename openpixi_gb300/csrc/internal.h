@@ -107,6 +107,15 @@ struct Ctx {
     // E there and the pointers swap), the transported Gauss-law terms of the
     // last and the next step, the block partials and the per-step rows
     void *E_alt = nullptr, *W_in = nullptr, *W_out = nullptr;
+    // per-site B_d^2 of Unext [3][V] (FP64) written by the generic BulkQuantities
+    // pass (null: not written), and the state it belongs to: ProjectedEnergyDensity
+    // after opx_reduce on the same state reads them instead of forming the
+    // plaquettes again
+    double *bn_site = nullptr;
+    struct {
+        long calls = -1, steps = -1;
+        const void *unext = nullptr;
+    } bnsite;
     double *meas_part = nullptr, *meas_rows = nullptr, *meas_host = nullptr;  // rows: device and pinned
     int meas_rows_cap = 0, meas_chunk = 0;  // steps whose partials meas_part holds
     bool profiling = false;
@@ -137,8 +146,9 @@ void launch_bulk(Ctx &c, int skip_u);
 int reduction_blocks(long V);
 void launch_energy_density(Ctx &c, double *dev_out);
 // six rows of dims[dir]: T_el, T_mag(U), L_el, L_mag(U), T_mag(Unext), L_mag(Unext)
-// (the U rows zero with skip_u)
-void launch_projected_energy(Ctx &c, int dir, int skip_u, double *dev_out);
+// (the U rows zero with skip_u); with bn_site the per-site B^2 of Unext come
+// from that buffer instead of the plaquettes
+void launch_projected_energy(Ctx &c, int dir, int skip_u, const double *bn_site, double *dev_out);
 int launch_projected_poynting(Ctx &c, int dir, double *dev_out);  // SU(2) only
 void launch_gauss_field(Ctx &c, double *dev_out);
 // ---- conversions (convert_kernels.cu) ----

@@ -68,7 +68,8 @@ template <int NC, typename R>
 __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     k_bulk_partial(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
                    const R *__restrict__ rho, const uint8_t *__restrict__ eval, Lat L, int skip_u,
-                   double *__restrict__ part, unsigned *__restrict__ count, double *__restrict__ out) {
+                   double *__restrict__ part, unsigned *__restrict__ count, double *__restrict__ out,
+                   double *__restrict__ bn_site) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
             }
             field_b<G, R>(Unp, L, s, nb, i, b1);
             const double bn = sqr<R, NA>(b1);
+            if (bn_site) bn_site[(long)i * L.V + s] = bn;
             if (i == 0) { p[0] += ev; p[3] += bu; p[8] += bn; }
             else if (i == 1) { p[1] += ev; p[4] += bu; p[9] += bn; }
             else { p[2] += ev; p[5] += bu; p[10] += bn; }
@@ -320,7 +322,7 @@ static void bulk_t(Ctx &c, int skip_u) {
         nb = std::min(nb, wave);
         k_bulk_partial<NC, R><<<nb, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
                                                                (const R *)c.rho, c.eval, c.L, skip_u, c.red_part,
-                                                               c.red_count, c.red_out);
+                                                               c.red_count, c.red_out, c.bn_site);
     }
     c.launches += 1;
 }
@@ -372,7 +374,8 @@ constexpr int PROJ_COLUMNS = 6;
 template <int NC, typename R>
 __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     k_projected_energy(const R *__restrict__ U, const R *__restrict__ Unext, const R *__restrict__ E,
-                       const uint8_t *__restrict__ eval, Lat L, int dir, int skip_u, double *__restrict__ part) {
+                       const uint8_t *__restrict__ eval, Lat L, int dir, int skip_u,
+                       const double *__restrict__ bn_site, double *__restrict__ part) {
     using G = typename GroupOf<NC, R>::T;
     constexpr int NA = G::NA;
     const LinkPlanes<G, R> Up{const_cast<R *>(U), L.V}, Unp{const_cast<R *>(Unext), L.V};
@@ -404,9 +407,15 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
                 field_b<G, R>(Up, L, s, nb, j, b0);
                 mu = 0.25 * sqr<R, NA>(b0) * uf;
             }
-            field_b<G, R>(Unp, L, s, nb, j, b1);
+            double bn;
+            if (bn_site) {
+                bn = __ldg(bn_site + (long)j * L.V + s);
+            } else {
+                field_b<G, R>(Unp, L, s, nb, j, b1);
+                bn = sqr<R, NA>(b1);
+            }
             const double el = 0.5 * sqr<R, NA>(e) * uf;
-            const double mn = 0.25 * sqr<R, NA>(b1) * uf;
+            const double mn = 0.25 * bn * uf;
             if (j == dir) { el_l += el; mu_l += mu; mn_l += mn; } else { el_t += el; mu_t += mu; mn_t += mn; }
         }
         two_sum_add(acc[0], el_t);
@@ -617,7 +626,7 @@ static void energy_density_t(Ctx &c, double *out) {
 void launch_energy_density(Ctx &c, double *out) { OPX_DISPATCH(energy_density_t, c, out); }
 
 template <int NC, typename R>
-static void projected_energy_t(Ctx &c, int dir, int skip_u, double *out) {
+static void projected_energy_t(Ctx &c, int dir, int skip_u, const double *bn_site, double *out) {
     // split each slice over enough blocks to fill the GPU, within the partial
     // buffer (2 * BULK_COLUMNS * max(red_blocks, 2 (n0 + n1 + n2)) doubles; 12
     // doubles per (slice, split))
@@ -628,12 +637,12 @@ static void projected_energy_t(Ctx &c, int dir, int skip_u, double *out) {
     nsplit = (int)std::min<long>(nsplit, cap / (2L * PROJ_COLUMNS * ns));
     nsplit = std::max(nsplit, 1);
     k_projected_energy<NC, R><<<dim3(ns, nsplit), RED_THREADS, 0, c.stream>>>(
-        (const R *)c.U, (const R *)c.Unext, (const R *)c.E, c.eval, c.L, dir, skip_u, c.red_part);
+        (const R *)c.U, (const R *)c.Unext, (const R *)c.E, c.eval, c.L, dir, skip_u, bn_site, c.red_part);
     k_projected_final<<<grid_for((long)PROJ_COLUMNS * ns, 128), 128, 0, c.stream>>>(c.red_part, ns, nsplit, out);
     c.launches += 2;
 }
-void launch_projected_energy(Ctx &c, int dir, int skip_u, double *out) {
-    OPX_DISPATCH(projected_energy_t, c, dir, skip_u, out);
+void launch_projected_energy(Ctx &c, int dir, int skip_u, const double *bn_site, double *out) {
+    OPX_DISPATCH(projected_energy_t, c, dir, skip_u, bn_site, out);
 }
 
 template <int NC, typename R>

@@ -127,3 +127,31 @@ def test_projected_energy_reuse_bit_identical(native, orc, nc, dims, prec):
             ref = g.projected_energy(d)
             got = a.projected_energy(d)
             assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), d
+
+
+@pytest.mark.parametrize("nc,dims,prec,masked", [
+    (2, (12, 8, 10), N.OPX_F64, False),
+    (2, (10, 9, 8), N.OPX_F64, True),
+    (3, (8, 10, 6), N.OPX_F64, False),
+    (2, (8, 12, 10), N.OPX_F32, False),
+])
+def test_projected_energy_from_reduction_sites(native, nc, dims, prec, masked):
+    """ProjectedEnergyDensity right after opx_reduce on the same state reads the
+    per-site B^2 of Unext that the BulkQuantities pass left (no plaquettes
+    formed again); a twin that calls it before the reduction forms them.  Rows
+    and observables bit-identical, with and without an evaluation region."""
+    g, (a, b) = twin_handles(nc, dims, prec, 0, 9, 0.3)
+    if masked:
+        m = (np.arange(a.V) % 7 != 2).astype(np.uint8)
+        a.set_evaluatable(m)
+        b.set_evaluatable(m)
+    for k in range(5):
+        oa = a.reduce()
+        pa = [a.projected_energy(d) for d in (0, 1)]
+        pb = [b.projected_energy(d) for d in (0, 1)]
+        ob = b.reduce()
+        assert np.array_equal(vec(oa), vec(ob)), k
+        for x, y in zip(pa, pb):
+            assert np.array_equal(x, y), k
+        a.step(1)
+        b.step(1)
