@@ -384,9 +384,12 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
     const int o1 = (dir + 1) % 3, o2 = (dir + 2) % 3;
     const long nt = L.V / L.n[dir];
     const double area = (double)L.V / (double)L.n[dir];
-    KSum acc[PROJ_COLUMNS];
+    // a thread's sites of the slice are summed plainly in FP64 (a handful per
+    // thread: nt / (nsplit * blockDim) of them), the block's threads with
+    // compensation; the FP64 pipe is narrow on this part
+    double p[PROJ_COLUMNS];
 #pragma unroll
-    for (int q = 0; q < PROJ_COLUMNS; q++) acc[q] = KSum{0.0, 0.0};
+    for (int q = 0; q < PROJ_COLUMNS; q++) p[q] = 0.0;
     for (long t = (long)blockIdx.y * blockDim.x + threadIdx.x; t < nt; t += (long)nsplit * blockDim.x) {
         int x[3];
         x[dir] = k;
@@ -418,15 +421,18 @@ __global__ void __launch_bounds__(RED_THREADS, RedBounds<NC, R>::minb)
             const double mn = 0.25 * bn * uf;
             if (j == dir) { el_l += el; mu_l += mu; mn_l += mn; } else { el_t += el; mu_t += mu; mn_t += mn; }
         }
-        two_sum_add(acc[0], el_t);
-        two_sum_add(acc[2], el_l);
-        two_sum_add(acc[4], mn_t);
-        two_sum_add(acc[5], mn_l);
+        p[0] += el_t;
+        p[2] += el_l;
+        p[4] += mn_t;
+        p[5] += mn_l;
         if (!skip_u) {
-            two_sum_add(acc[1], mu_t);
-            two_sum_add(acc[3], mu_l);
+            p[1] += mu_t;
+            p[3] += mu_l;
         }
     }
+    KSum acc[PROJ_COLUMNS];
+#pragma unroll
+    for (int q = 0; q < PROJ_COLUMNS; q++) acc[q] = KSum{p[q], 0.0};
     int q;
     KSum v = block_reduce<PROJ_COLUMNS>(acc, q);
     if (q >= 0) {
