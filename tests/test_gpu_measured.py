@@ -68,6 +68,7 @@ RTOL_GAUSS = 1e-5
     ((16, 16, 16), 4, False, 0.05),   # reunitarisation steps inside the run
     ((12, 10, 14), 0, True, 0.0),     # V = 1680: the last thread has one site; a static charge density
     ((24, 20, 16), 3, False, 0.05),
+    ((3, 2, 5), 0, False, 0.05),      # V = 30: one warp, every thread with one site
 ])
 def test_fused_rows_match_step_and_reduce(native, dims, reunit, rho, kick):
     a, b = twins(3, dims, N.OPX_F32, reunit, rho=rho, kick=kick)
