@@ -206,6 +206,28 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo; Arm hosts report
+    the implementer and part numbers there)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        info = open("/proc/cpuinfo").read()
+    except OSError:
+        return "unknown"
+    for line in info.splitlines():
+        if line.lower().startswith("model name"):
+            return line.split(":", 1)[1].strip()
+    impl = [ln.split(":", 1)[1].strip() for ln in info.splitlines() if ln.startswith("CPU implementer")]
+    part = [ln.split(":", 1)[1].strip() for ln in info.splitlines() if ln.startswith("CPU part")]
+    return f"Arm implementer {impl[0]} part {part[0]}" if impl and part else "unknown"
+
+
 def cpu_baseline(w, U_ref, E_ref, target_s=12.0):
     """The oracle (FP64 restatement of the reference update, C + OpenMP) on a bounded
     sample of the same lattice: whole-lattice steps, or a leading slab of sites when
@@ -226,6 +248,7 @@ def cpu_baseline(w, U_ref, E_ref, target_s=12.0):
     g.update_grid_range_omp(0, sites, nth)
     el = time.perf_counter() - t
     return {"value": 3.0 * sites / el, "unit": METRIC, "cores": nth, "kind": "port",
+            "cpu_model": cpu_model(), "build": "gcc -O3 -fopenmp -ffp-contract=off",
             "sample": f"one leapfrog update of {planes} of {w['dims'][0]} x0-planes ({sites} sites, "
                       f"{3 * sites} link updates) of the same lattice, FP64, {nth} OpenMP threads, {el:.2f} s"}
 
@@ -261,7 +284,9 @@ def run_reference(args, w, wname):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_for(w, wname),
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nth, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nth, "kind": "port",
+                             "cpu_model": cpu_model(), "build": "gcc -O3 -fopenmp -ffp-contract=off",
+                             "sample": sample},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

@@ -370,7 +370,13 @@ long opx_batch_kernel_launches(const opx_batch *b);
  * array of the library, held by every GPU that loads the library until exit.
  * Limit: V <= 2^29 sites (larger lattices return OPX_ERR_INVALID).  The first
  * call on a device looks up the scratch address and should come before any
- * stream capture.  Calls share the scratch, so calls that overlap on the GPU race. */
+ * stream capture; after cudaDeviceReset of a device the looked-up address is
+ * stale, so do not call it on that device again.  Calls share the scratch, so
+ * calls that overlap on the GPU race.  Non-finite field values are not
+ * detected (opx_reduce returns OPX_ERR_NUMERIC for them): they reach the record
+ * as NaN or Inf, and the caller checks it.  OPX_ERR_CUDA reports a launch
+ * failure of this call only; an error left pending by earlier work is neither
+ * reported nor cleared. */
 int opx_reduce_noalloc(int ncolors, int precision, const int *dims, const double *a, double g,
                        const void *U, const void *Unext, const void *E, const void *rho,
                        const uint8_t *eval, opx_observables *out_device, void *stream);

@@ -8,6 +8,17 @@
 // log(1+f) = f - s (f - R(s^2)) with fdlibm's minimax polynomial R, and k ln2
 // split into a high and a low part.  Compile without floating-point
 // contraction (-ffp-contract=off) so that every host gives the same bits.
+//
+// fdlibm_log restates fdlibm's e_log.c (its constants and reduction steps),
+// which carries this notice:
+// ====================================================
+// Copyright (C) 1993 by Sun Microsystems, Inc. All rights reserved.
+//
+// Developed at SunSoft, a Sun Microsystems, Inc. business.
+// Permission to use, copy, modify, and distribute this
+// software is freely granted, provided that this notice
+// is preserved.
+// ====================================================
 #pragma once
 #include <cmath>
 #include <cstdint>

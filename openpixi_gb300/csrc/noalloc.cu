@@ -21,7 +21,11 @@
 // stream capture.  Every call reuses the same array: calls that overlap on the
 // GPU (on different streams, or from different host threads) race on it.  Each
 // block overwrites its own partials before the final kernel reads them, so no
-// part of the array has to start at zero.
+// part of the array has to start at zero.  The cached address belongs to the
+// device's context: after cudaDeviceReset on a device it is stale, so a process
+// that resets a device must not call this entry point on that device again.
+// Unlike opx_reduce, non-finite field values are not turned into an error
+// status; they reach the record as NaN or Inf, and the caller checks it.
 #include <mutex>
 
 #include "internal.h"
@@ -128,6 +132,8 @@ extern "C" int opx_reduce_noalloc(int ncolors, int precision, const int *dims, c
     const Lat L = make_lat(dims, a, 1.0, g);
     const int nblocks = (int)std::min<long>((V + 255) / 256, OPX_NOALLOC_BLOCKS);
     cudaStream_t st = (cudaStream_t)stream;
+    // an error left pending by earlier work of the caller is neither reported nor cleared here
+    const cudaError_t pending = cudaPeekAtLastError();
     if (ncolors == 2) {
         if (precision == OPX_F64) noalloc_launch<2, double>(L, U, Unext, E, rho, eval, part, nblocks, out_device, st);
         else noalloc_launch<2, float>(L, U, Unext, E, rho, eval, part, nblocks, out_device, st);
@@ -135,5 +141,10 @@ extern "C" int opx_reduce_noalloc(int ncolors, int precision, const int *dims, c
         if (precision == OPX_F64) noalloc_launch<3, double>(L, U, Unext, E, rho, eval, part, nblocks, out_device, st);
         else noalloc_launch<3, float>(L, U, Unext, E, rho, eval, part, nblocks, out_device, st);
     }
-    return cudaGetLastError() == cudaSuccess ? OPX_OK : OPX_ERR_CUDA;
+    const cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess && e != pending) {
+        (void)cudaGetLastError();  // this call's launch error: consumed and reported
+        return OPX_ERR_CUDA;
+    }
+    return OPX_OK;
 }

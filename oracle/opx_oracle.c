@@ -1368,7 +1368,16 @@ typedef struct { uint64_t seed; int have; double next; } jrand;
 /* StrictMath.log: the fdlibm algorithm (e_log.c, the method Java specifies for
  * StrictMath): x = 2^k (1+f) with sqrt(2)/2 < 1+f < sqrt(2), s = f/(2+f),
  * log(1+f) = f - s (f - R(s^2)) with a degree-14 even minimax polynomial R,
- * and k ln2 split into a high and a low part.  Finite x > 0 only. */
+ * and k ln2 split into a high and a low part.  Finite x > 0 only.
+ * The constants and steps are fdlibm's e_log.c, which carries this notice:
+ * ====================================================
+ * Copyright (C) 1993 by Sun Microsystems, Inc. All rights reserved.
+ *
+ * Developed at SunSoft, a Sun Microsystems, Inc. business.
+ * Permission to use, copy, modify, and distribute this
+ * software is freely granted, provided that this notice
+ * is preserved.
+ * ==================================================== */
 static double strict_log(double x)
 {
     static const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10,

@@ -44,16 +44,26 @@ def link_blocks(arr):
     return np.ascontiguousarray(pad.reshape(nb, 32, 3, ng).transpose(2, 0, 3, 1))
 
 
-@pytest.mark.parametrize("nc,prec", [(3, N.OPX_F32), (2, N.OPX_F64)])
-def test_noalloc_matches_reduce(native, nc, prec):
+CASES = [(nc, prec, form) for nc in (2, 3) for prec in (N.OPX_F64, N.OPX_F32) for form in ("rho", "eval")]
+
+
+@pytest.mark.parametrize("nc,prec,form", CASES)
+def test_noalloc_matches_reduce(native, nc, prec, form):
+    """form "rho": a charge density and every cell evaluated; form "eval": no
+    charge (rho = NULL) and an evaluation mask, passed to both entry points."""
     torch = pytest.importorskip("torch")
     dims = (12, 10, 14)
     h = opx.Handle(nc, dims, dt=0.05, precision=prec, reunit_every=10 if prec == N.OPX_F32 else 0)
     h.init_random(31, 0.3, 0.3)
     h.gauss_project(1e-24)
     rng = np.random.default_rng(4)
-    rho = rng.normal(0, 0.05, (h.V, h.ngen))
-    h.upload(N.FIELD_RHO, rho, layout=N.LAYOUT_GEN)
+    mask = None
+    if form == "rho":
+        rho = rng.normal(0, 0.05, (h.V, h.ngen))
+        h.upload(N.FIELD_RHO, rho, layout=N.LAYOUT_GEN)
+    else:
+        mask = (rng.random(h.V) < 0.6).astype(np.uint8)
+        h.set_evaluatable(mask)
     h.initialize()
     h.step(3)
     ref = as_vec(h.reduce())
@@ -63,18 +73,30 @@ def test_noalloc_matches_reduce(native, nc, prec):
     U = torch.from_numpy(link_blocks(h.download(N.FIELD_U))).to(dev, dt)
     Un = torch.from_numpy(link_blocks(h.download(N.FIELD_UNEXT))).to(dev, dt)
     E = torch.from_numpy(planes(h.download(N.FIELD_E, layout=N.LAYOUT_GEN), 3)).to(dev, dt)
-    R = torch.from_numpy(planes(h.download(N.FIELD_RHO, layout=N.LAYOUT_GEN), 0)).to(dev, dt)
+    R = None
+    if form == "rho":
+        R = torch.from_numpy(planes(h.download(N.FIELD_RHO, layout=N.LAYOUT_GEN), 0)).to(dev, dt)
+    M = None if mask is None else torch.from_numpy(mask).to(dev)
     out = torch.full((13,), float("nan"), dtype=torch.float64, device=dev)
     dims_c = (C.c_int * 3)(*dims)
     a_c = (C.c_double * 3)(1.0, 1.0, 1.0)
     stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def call():
+        return native.opx_reduce_noalloc(nc, prec, dims_c, a_c, 1.0, C.c_void_p(U.data_ptr()),
+                                         C.c_void_p(Un.data_ptr()), C.c_void_p(E.data_ptr()),
+                                         None if R is None else C.c_void_p(R.data_ptr()),
+                                         None if M is None else C.c_void_p(M.data_ptr()),
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+
+    # a first call loads the kernels and looks up the scratch address; the two
+    # calls checked after it must leave the device's free memory unchanged
+    assert call() == N.OPX_OK
+    torch.cuda.synchronize(dev)
+    free_before = torch.cuda.mem_get_info(dev)[0]
     for _ in range(2):
         out.fill_(float("nan"))
-        rc = native.opx_reduce_noalloc(nc, prec, dims_c, a_c, 1.0, C.c_void_p(U.data_ptr()),
-                                       C.c_void_p(Un.data_ptr()), C.c_void_p(E.data_ptr()),
-                                       C.c_void_p(R.data_ptr()), None, C.c_void_p(out.data_ptr()),
-                                       C.c_void_p(stream))
-        assert rc == N.OPX_OK
+        assert call() == N.OPX_OK
         torch.cuda.synchronize(dev)
         got = out.cpu().numpy()
         assert np.all(np.isfinite(got))
@@ -82,11 +104,17 @@ def test_noalloc_matches_reduce(native, nc, prec):
         # SU(3) FP32 kernel, in another operation order (FP32 rounding)
         rtol = 1e-6 if prec == N.OPX_F32 else 1e-12
         assert np.allclose(got, ref, rtol=rtol, atol=1e-300), (got, ref)
+    assert torch.cuda.mem_get_info(dev)[0] == free_before
 
 
 def test_noalloc_rejects_oversize(native):
+    """Sizes beyond the limit are refused before anything is launched; the
+    buffers passed are real (small) device buffers all the same."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    buf = torch.zeros(64, dtype=torch.float64, device=dev)
+    p = C.c_void_p(buf.data_ptr())
     dims_c = (C.c_int * 3)(1024, 1024, 1024)
     a_c = (C.c_double * 3)(1.0, 1.0, 1.0)
-    rc = native.opx_reduce_noalloc(2, N.OPX_F64, dims_c, a_c, 1.0, C.c_void_p(8), C.c_void_p(8),
-                                   C.c_void_p(8), None, None, C.c_void_p(8), None)
+    rc = native.opx_reduce_noalloc(2, N.OPX_F64, dims_c, a_c, 1.0, p, p, p, None, None, p, None)
     assert rc == N.OPX_ERR_INVALID
