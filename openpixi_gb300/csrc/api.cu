@@ -127,6 +127,7 @@ int opx_create(const opx_config *cfg, opx_ctx **out) {
     c.na_ref = c.nc == 3 ? 9 : 3;
     c.prec = cfg->precision;
     c.pair_kernel = std::getenv("OPX_ONE_SITE_FP32") == nullptr;
+    c.stream_kernel = std::getenv("OPX_STREAM_FP32") != nullptr;
     c.int_offsets = std::getenv("OPX_LONG_OFFSETS") == nullptr && link_elems(V, c.ng) < (1L << 31) - 64 &&
                     3L * c.na * V < (1L << 31);
     c.rsize = c.prec == OPX_F64 ? 8 : 4;

@@ -13,10 +13,14 @@
 // Unext_i(x); the 12 neighbour links of the staples are served from L1/L2
 // (consecutive blocks cover consecutive sites, so the +-1 planes of dimension
 // 0 are resident in L2 while a block works on its plane).
+#include <algorithm>
+#include <cstdlib>
+
 #include "internal.h"
 #include "leapfrog.cuh"
 #include "su3_log.cuh"
 #include "su3_pair.cuh"
+#include "su3_stream.cuh"
 
 namespace opx {
 
@@ -361,7 +365,41 @@ static void update_grid_su3f_pair_i(Ctx &c, bool reunit) {
     c.launches++;
 }
 
+// The plaquette form streamed along dimension 0 (su3_stream.cuh): one wave of
+// resident blocks, each with an equal share of the (tile, x0) units.
+static bool stream_eligible(const Ctx &c) {
+    return c.stream_kernel && c.int_offsets && !c.j_nonzero && !c.active && c.L.n[1] % st::T1 == 0 &&
+           c.L.n[2] % st::T2 == 0;
+}
+
+static void update_grid_su3f_stream(Ctx &c, bool reunit) {
+    const int smem = (int)sizeof(st::Smem);
+    if (!c.st_grid) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(st::k_update_grid_su3f_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(st::k_update_grid_su3f_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, st::k_update_grid_su3f_stream<false>, st::THREADS, smem);
+        const long units = (long)(c.L.n[1] / st::T1) * (c.L.n[2] / st::T2) * c.L.n[0];
+        long grid = (long)std::max(1, per_sm) * std::max(1, sms);
+        // OPX_STREAM_BLOCKS=n: n blocks instead of one resident wave (tests use
+        // a few blocks so that each walks long ranges across tile boundaries)
+        if (const char *v = std::getenv("OPX_STREAM_BLOCKS")) grid = std::max(1L, std::atol(v));
+        c.st_grid = (int)std::max(1L, std::min<long>(units, grid));
+    }
+    const float *U = (const float *)c.U;
+    float *E = (float *)c.E, *Un = (float *)c.Unext;
+    if (reunit) st::k_update_grid_su3f_stream<true><<<c.st_grid, st::THREADS, smem, c.stream>>>(U, E, Un, c.L);
+    else st::k_update_grid_su3f_stream<false><<<c.st_grid, st::THREADS, smem, c.stream>>>(U, E, Un, c.L);
+    c.launches++;
+}
+
 static void update_grid_su3f_pair(Ctx &c, bool reunit) {
+    if (stream_eligible(c)) {
+        update_grid_su3f_stream(c, reunit);
+        return;
+    }
     // 32-bit offsets while the largest link offset (3 blocks x 576 floats) fits
     if (c.int_offsets) update_grid_su3f_pair_i<int>(c, reunit);
     else update_grid_su3f_pair_i<long>(c, reunit);

@@ -60,6 +60,13 @@ struct Ctx {
     // and E offset fits (SU(3): 54 V < 2^31); OPX_LONG_OFFSETS=1 selects the
     // 64-bit forms at any size, so that tests can compare them on small lattices
     bool int_offsets = true;
+    // opt-in (OPX_STREAM_FP32=1): the SU(3) FP32 leapfrog in plaquette form
+    // streamed along dimension 0 (su3_stream.cuh), where the lattice tiles
+    // (N1 % 8 == 0, N2 % 32 == 0) and there is no current or activity mask.
+    // st_grid: its resident-wave grid (0 = not yet computed for this handle's
+    // device)
+    bool stream_kernel = false;
+    int st_grid = 0;
     double *staging = nullptr;
     size_t staging_len = 0;  // doubles
     double *red_part = nullptr;

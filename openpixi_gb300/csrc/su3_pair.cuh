@@ -34,7 +34,16 @@ __device__ __forceinline__ P fma2(P a, P b, P c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ P mul2(P a, P b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ P add2(P a, P b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ P neg2(P a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ P sub2(P a, P b) { return __fadd2_rn(a, neg2(b)); }
+// a - b in one paired instruction (sub.rn.f32x2; the same bits as a + (-b))
+__device__ __forceinline__ P sub2(P a, P b) {
+    unsigned long long ra, rb, rc;
+    memcpy(&ra, &a, 8);
+    memcpy(&rb, &b, 8);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rc) : "l"(ra), "l"(rb));
+    P c;
+    memcpy(&c, &rc, 8);
+    return c;
+}
 __device__ __forceinline__ P zero2() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ float maxl(P a) { return fmaxf(a.x, a.y); }
 // the sum of the lanes whose site counts

@@ -101,9 +101,13 @@ def test_noalloc_matches_reduce(native, nc, prec, form):
         got = out.cpu().numpy()
         assert np.all(np.isfinite(got))
         # FP32 storage: opx_reduce forms the per-site values with the paired
-        # SU(3) FP32 kernel, in another operation order (FP32 rounding)
-        rtol = 1e-6 if prec == N.OPX_F32 else 1e-12
-        assert np.allclose(got, ref, rtol=rtol, atol=1e-300), (got, ref)
+        # SU(3) FP32 kernel, in another operation order (FP32 rounding); the
+        # Gauss column of a projected FP32 state without charge is rounding
+        # noise (~1e-14), compared on the absolute scale of the energy
+        if prec == N.OPX_F32:
+            assert np.allclose(got, ref, rtol=1e-6, atol=1e-12 * abs(ref[-2] + ref[-1])), (got, ref)
+        else:
+            assert np.allclose(got, ref, rtol=1e-12, atol=1e-300), (got, ref)
     assert torch.cuda.mem_get_info(dev)[0] == free_before
 
 
