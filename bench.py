@@ -301,19 +301,22 @@ def config_for(w, wname):
             else "lattice fits in L2", "parallelism": "replicas (one lattice per GPU)"}
 
 
-def bench_batch(device, nsteps=200, nev=256, seed=SEED):
-    """Batching form: 256 SU(2) events of cubic sizes drawn uniformly from
-    {16,24,32,40,48}^3, FP32 with reunitarisation every 10 steps, 200 steps in
-    one persistent launch replayed from a CUDA graph (autotuned cluster / block
-    size), against the plain FP64 single-lattice path looping over the same
-    events (GPU time of each event's 200 steps, summed), which also gives the
-    batch's energy error after 200 steps (max over the events)."""
+def bench_batch(device, nc=2, nsteps=200, nev=256, seed=SEED):
+    """Batching form: 256 events of cubic sizes drawn uniformly from
+    {16,24,32,40,48}^3 (SU(2), the configured workload; SU(3) with the same
+    sizes, seeds and widths beside it), FP32 with reunitarisation every 10
+    steps, 200 steps in one persistent launch replayed from a CUDA graph
+    (autotuned cluster / block size), against the plain FP64 single-lattice path
+    looping over the same events (GPU time of each event's 200 steps, summed),
+    which also gives the batch's energy error after 200 steps (max over the
+    events)."""
     import openpixi_gb300 as opx
     from openpixi_gb300 import _native as N
     rng = np.random.default_rng(seed)
     sizes = [int(x) for x in rng.choice([16, 24, 32, 40, 48], nev)]
     dims = [(L, L, L) for L in sizes]
-    b = opx.Batch(2, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
+    bpl = 56 if nc == 2 else 208
+    b = opx.Batch(nc, dims, dt=0.05, precision=N.OPX_F32, reunit_every=10, device=device)
     b.init_random([seed + 1000 + q for q in range(nev)], 0.1, 0.1, tol=1e-24)
     b.initialize()
     init = [(b.download(q, N.FIELD_U), b.download(q, N.FIELD_E)) for q in range(nev)]
@@ -334,7 +337,7 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
     for q, d in enumerate(dims):
         h = handles.get(d)
         if h is None:
-            h = handles[d] = opx.Handle(2, d, dt=0.05, precision=N.OPX_F64, device=device)
+            h = handles[d] = opx.Handle(nc, d, dt=0.05, precision=N.OPX_F64, device=device)
         h.upload(N.FIELD_U, init[q][0])
         h.upload(N.FIELD_E, init[q][1])
         h.initialize()
@@ -347,9 +350,10 @@ def bench_batch(device, nsteps=200, nev=256, seed=SEED):
     peak, _ = hbm_peak()
     lu = links * nsteps / (ms / 1000.0)
     b.close()
-    return {"events": nev, "steps": nsteps, "lattice_sizes": "L^3, L uniform in {16,24,32,40,48}",
+    return {"group": f"SU({nc})", "events": nev, "steps": nsteps,
+            "lattice_sizes": "L^3, L uniform in {16,24,32,40,48}",
             "link_updates_per_step": links, "ms": ms, "events_per_s": nev / (ms / 1000.0),
-            "link_updates_per_s": lu, "roofline_frac": 56.0 * lu / 1e9 / peak, "bytes_per_link": 56,
+            "link_updates_per_s": lu, "roofline_frac": bpl * lu / 1e9 / peak, "bytes_per_link": bpl,
             "fp64_loop_ms": ms64, "fp64_loop_events_per_s": nev / (ms64 / 1000.0),
             "speedup_vs_fp64_loop": ms64 / ms, "cluster": cluster, "block": block, "graph": True,
             "gpu_launches": launches, "max_gauss": max(o.gauss for o in obs),
@@ -408,11 +412,19 @@ def bench_cgc(device, nsteps=300, oracle_steps=2):
     step_ms = (ms[N.PHASE_EOM] + ms[N.PHASE_CPIC]) / nsteps
     peak, _ = hbm_peak()
     lu = links / (step_ms / 1000.0)
+    # algorithmic bytes of the particle phases per step (SU(2) FP64): per particle
+    # the state read (pos, vel, Q0, Q1: 96 B, direction 1 B) and written (pos0,
+    # pos1, Q0, Q1: 96 B) and, on a cell change, one Unext link (32 B; with
+    # |v| = 1 and dt = a/2 every particle changes cell every other step); per
+    # site the rho (24 B) and J (72 B) written
+    cpic_bytes = np_ * (193 + 0.5 * 32) + int(np.prod(CGC_DIMS)) * 96
+    cpic_ms = ms[N.PHASE_CPIC] / nsteps
     out = {"workload": "SU(2) CPIC collision, 256x64^2, dt=0.5, 2 MV nuclei, FP64", "particles": np_,
            "steps": nsteps, "ic_ms": ic_ms, "wall_ms_with_diagnostics": wall_ms,
            "ms_per_step_device": step_ms, "eom_ms_per_step": ms[N.PHASE_EOM] / nsteps,
            "cpic_ms_per_step": ms[N.PHASE_CPIC] / nsteps, "diagnostics_ms_per_step": ms[N.PHASE_DIA] / nsteps,
-           "link_updates_per_s": lu, "particle_updates_per_s": np_ / (ms[N.PHASE_CPIC] / nsteps / 1000.0),
+           "link_updates_per_s": lu, "particle_updates_per_s": np_ / (cpic_ms / 1000.0),
+           "cpic_bytes_per_step": cpic_bytes, "roofline_frac_cpic": cpic_bytes / (cpic_ms / 1000.0) / 1e9 / peak,
            "roofline_frac_eom": 136.0 * links / (ms[N.PHASE_EOM] / nsteps / 1000.0) / 1e9 / peak,
            "bytes_per_link": 136, "max_gauss_mean_sq": gmax, "energy_start": e0, "energy_end": e1,
            "projected_energy_rows": [4, CGC_DIMS[0]], "final_T_el_sum": float(proj[-1][0].sum())}
@@ -522,9 +534,36 @@ def bench_differentiation(device, ndir=64):
         worst["tl"] = max(worst["tl"], abs(adj - dJ) / abs(dJ))
         worst["f32_vs_tl"] = max(worst["f32_vs_tl"], abs(float((g32 * d).sum()) - dJ) / abs(dJ))
     tcheck = time.perf_counter() - t
+    # the other objective / input pairs on the same workload, checked on 8
+    # unit-norm directions each (central differences h = 1e-4, tangent-linear)
+    forms = {}
+    for name, kind, wrt in (("anisotropy_wrt_E", N.OBJ_ANISOTROPY, N.WRT_E),
+                            ("energy_wrt_rho", N.OBJ_ENERGY, N.WRT_RHO),
+                            ("anisotropy_wrt_rho", N.OBJ_ANISOTROPY, N.WRT_RHO)):
+        t = time.perf_counter()
+        Jf, gf = h64.objective_gradient(nsteps, ckpt, kind, 0, lo, hi, wrt)
+        tg = time.perf_counter() - t
+        wf = {"fd": 0.0, "tl": 0.0}
+        rng_f = np.random.default_rng(100 + kind + 2 * wrt)
+        for _ in range(8):
+            d = rng_f.normal(size=gf.shape)
+            d /= np.linalg.norm(d)
+            adj = float((gf * d).sum())
+            kw = {"dE": d} if wrt == N.WRT_E else {"drho": d}
+            fd = (h64.objective_value(nsteps, kind, 0, lo, hi, h=1e-4, **kw) -
+                  h64.objective_value(nsteps, kind, 0, lo, hi, h=-1e-4, **kw)) / 2e-4
+            _, dJ = h64.objective_tangent(nsteps, kind, 0, lo, hi, **kw)
+            wf["fd"] = max(wf["fd"], abs(fd - adj) / abs(adj))
+            wf["tl"] = max(wf["tl"], abs(adj - dJ) / abs(dJ))
+        forms[name] = {"J": Jf, "gradient_s_fp64_forward": tg, "directions": 8,
+                       "worst_rel_vs_central_fd": wf["fd"], "worst_rel_vs_tangent_linear": wf["tl"]}
     h64.close()
     h32.close()
     return {"workload": "SU(2) 64^3, 200 steps, dt=0.05, ckpt 14, central 16^3 energy density",
+            "other_forms": forms,
+            "other_forms_note": "anisotropy = sum P_L / sum P_T of the projected components over the same box, "
+                                "longitudinal direction 0; rho enters through the Gauss projection of the "
+                                "initial E (dJ/drho = K^+ div dJ/dE_0)",
             "J": J64, "gradient_s_fp32_forward": t32, "gradient_s_fp64_forward": t64,
             "directions": ndir, "worst_rel_vs_central_fd": worst["fd"],
             "worst_rel_vs_central_fd_unit_rms_direction": worst["fd_rms"],
@@ -804,7 +843,8 @@ def main():
 
     batched = None
     if not args.no_batch and args.workload == "su3_fp32_128":
-        batched = bench_batch(device)
+        batched = bench_batch(device, nc=2)
+        batched["su3"] = bench_batch(device, nc=3)
 
     cgc = None
     if not args.no_cgc and args.workload == "su3_fp32_128":

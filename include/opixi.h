@@ -323,6 +323,43 @@ int opx_energy_tangent(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, c
 int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const int *hi, double *J,
                         double *grad, size_t count);
 
+/* The general form: an objective selector and the charge density as a second
+ * input.
+ *   OPX_OBJ_ENERGY     the mean EnergyDensity over the box (as above);
+ *   OPX_OBJ_ANISOTROPY the pressure anisotropy P_L / P_T over the box from the
+ *     components of ProjectedEnergyDensity (diagnostics/methods/
+ *     ProjectedEnergyDensity.java:18-41, 114-179) with `direction` the
+ *     longitudinal axis: per cell and direction j, eps_j = [E_j^2/2 +
+ *     (|B_j(U)|^2 + |B_j(Unext)|^2)/4] / (g a_j)^2, eps_L = eps_direction,
+ *     eps_T = the other two, P_L = eps_T - eps_L, P_T = eps_L, and
+ *     J = sum_box P_L / sum_box P_T.
+ * Inputs: OPX_WRT_E, the initial E ([V][3][3] generator components); or
+ * OPX_WRT_RHO, the colour-charge density ([V][3]) through Gauss's law
+ * (Grid.getGaussConstraint, physics/grid/Grid.java:944-968): the initial E is
+ * the projection of the handle's E onto div E = rho (opx_gauss_project), so a
+ * change d of rho moves E_0 by divT K^+ d (K = div divT on the handle's links)
+ * and dJ/drho = K^+ div dJ/dE_0.  The handle's E must satisfy Gauss's law for
+ * its rho (e.g. after opx_gauss_project).  SU(2) only; the handle's fields are
+ * not modified. */
+#define OPX_OBJ_ENERGY 0
+#define OPX_OBJ_ANISOTROPY 1
+#define OPX_WRT_E 0
+#define OPX_WRT_RHO 1
+typedef struct {
+    int kind;       /* OPX_OBJ_ENERGY or OPX_OBJ_ANISOTROPY */
+    int direction;  /* longitudinal axis of OPX_OBJ_ANISOTROPY (0, 1 or 2) */
+    int lo[3], hi[3];  /* the box of cells, inclusive */
+} opx_objective;
+/* J with E_0 moved by h (dE + divT K^+ drho) (dE, drho may be NULL): finite differences */
+int opx_objective_value(opx_ctx *ctx, const opx_objective *obj, int nsteps, const double *dE, const double *drho,
+                        double h, double *J);
+/* FP64 tangent-linear run along dE + divT K^+ drho (at least one non-NULL) */
+int opx_objective_tangent(opx_ctx *ctx, const opx_objective *obj, int nsteps, const double *dE, const double *drho,
+                          double *J, double *dJ);
+/* Adjoint gradient with respect to OPX_WRT_E (count = V*3*3) or OPX_WRT_RHO (count = V*3) */
+int opx_objective_gradient(opx_ctx *ctx, const opx_objective *obj, int nsteps, int ckpt, int wrt, double *J,
+                           double *grad, size_t count);
+
 /* ---- batching form: many independent lattices ("events") in one launch ----
  * The reference runs one Simulation per event (a loop over independent
  * Simulation objects); here every event advances in one persistent launch of

@@ -38,6 +38,7 @@ EXPORTED = [
     "opx_init_random", "opx_gauss_project",
     "opx_set_profiling", "opx_phase_times", "opx_time_steps", "opx_kernel_launches",
     "opx_host_alloc", "opx_host_free", "opx_reduce_noalloc",
+    "opx_objective_value", "opx_objective_tangent", "opx_objective_gradient",
     "opx_batch_create", "opx_batch_destroy", "opx_batch_last_error", "opx_batch_init_random",
     "opx_batch_upload", "opx_batch_download", "opx_batch_initialize", "opx_batch_autotune",
     "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
@@ -85,6 +86,15 @@ class Particles(C.Structure):
 
 
 _lib = None
+
+
+OBJ_ENERGY, OBJ_ANISOTROPY = 0, 1
+WRT_E, WRT_RHO = 0, 1
+
+
+class Objective(C.Structure):
+    """opx_objective: objective kind, longitudinal direction, box of cells."""
+    _fields_ = [("kind", C.c_int), ("direction", C.c_int), ("lo", C.c_int * 3), ("hi", C.c_int * 3)]
 
 
 def load(path=None):
@@ -158,6 +168,9 @@ def load(path=None):
         "opx_energy_objective": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, dp]),
         "opx_energy_tangent": (C.c_int, [vp, C.c_int, vp, vp, vp, dp, dp]),
         "opx_energy_gradient": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, dp, vp, sz]),
+        "opx_objective_value": (C.c_int, [vp, C.POINTER(Objective), C.c_int, vp, vp, C.c_double, dp]),
+        "opx_objective_tangent": (C.c_int, [vp, C.POINTER(Objective), C.c_int, vp, vp, dp, dp]),
+        "opx_objective_gradient": (C.c_int, [vp, C.POINTER(Objective), C.c_int, C.c_int, C.c_int, dp, vp, sz]),
         "opx_reduce_noalloc": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                          C.c_double, vp, vp, vp, vp, vp, vp, vp]),
     }
@@ -406,7 +419,8 @@ class Handle:
     def super_download(self, g):
         o, n, b = C.c_int(), C.c_long(), C.c_long()
         self.check(self.L.opx_super_download(self.h, int(g), C.byref(o), C.byref(n), C.byref(b), None, 0))
-        ppc = int(round(self.a[0] / self.dt))
+        from .diagnostics import java_round
+        ppc = java_round(self.a[0] / self.dt)  # LightConeNGPParticleCreator.java:89
         Q = np.empty((ppc, n.value, self.na_ref))
         self.check(self.L.opx_super_download(self.h, int(g), None, None, None, ptr(Q), Q.size))
         return {"orientation": o.value, "n": n.value, "base": b.value, "Q": Q}
@@ -441,6 +455,40 @@ class Handle:
         g = np.empty((self.V, 3, self.ngen))
         J = C.c_double()
         self.check(self.L.opx_energy_gradient(self.h, int(nsteps), int(ckpt), lo_c, hi_c, C.byref(J), ptr(g), g.size))
+        return J.value, g
+
+    def _objective(self, kind, direction, lo, hi):
+        lo = (0, 0, 0) if lo is None else lo
+        hi = tuple(d - 1 for d in self.dims) if hi is None else hi
+        return Objective(int(kind), int(direction), (C.c_int * 3)(*[int(v) for v in lo]),
+                         (C.c_int * 3)(*[int(v) for v in hi]))
+
+    def objective_value(self, nsteps, kind=OBJ_ENERGY, direction=0, lo=None, hi=None, dE=None, drho=None, h=0.0):
+        """J of the objective after nsteps, with E_0 moved by h (dE + divT K^+ drho)."""
+        ob = self._objective(kind, direction, lo, hi)
+        d = None if dE is None else np.ascontiguousarray(dE, dtype=np.float64)
+        r = None if drho is None else np.ascontiguousarray(drho, dtype=np.float64)
+        J = C.c_double()
+        self.check(self.L.opx_objective_value(self.h, C.byref(ob), int(nsteps), ptr(d), ptr(r), float(h),
+                                              C.byref(J)))
+        return J.value
+
+    def objective_tangent(self, nsteps, kind=OBJ_ENERGY, direction=0, lo=None, hi=None, dE=None, drho=None):
+        ob = self._objective(kind, direction, lo, hi)
+        d = None if dE is None else np.ascontiguousarray(dE, dtype=np.float64)
+        r = None if drho is None else np.ascontiguousarray(drho, dtype=np.float64)
+        J, dJ = C.c_double(), C.c_double()
+        self.check(self.L.opx_objective_tangent(self.h, C.byref(ob), int(nsteps), ptr(d), ptr(r), C.byref(J),
+                                                C.byref(dJ)))
+        return J.value, dJ.value
+
+    def objective_gradient(self, nsteps, ckpt, kind=OBJ_ENERGY, direction=0, lo=None, hi=None, wrt=WRT_E):
+        """(J, dJ/dE_0 [V][3][ngen]) or (J, dJ/drho [V][ngen])."""
+        ob = self._objective(kind, direction, lo, hi)
+        g = np.empty((self.V, 3, self.ngen)) if wrt == WRT_E else np.empty((self.V, self.ngen))
+        J = C.c_double()
+        self.check(self.L.opx_objective_gradient(self.h, C.byref(ob), int(nsteps), int(ckpt), int(wrt), C.byref(J),
+                                                 ptr(g), g.size))
         return J.value, g
 
     # ---- timing ----

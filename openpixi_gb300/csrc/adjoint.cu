@@ -1,9 +1,19 @@
 // adjoint.cu -- differentiation form of the SU(2) leapfrog.
 //
-// Objective: the mean of the per-cell energy density (EnergyDensity.ComponentComputation,
-// diagnostics/methods/EnergyDensity.java:119-166) over a box of cells after N
-// steps of Simulation.step, J = mean_x sum_d [E_d^2/2 + |B_d(U) + B_d(Unext)|^2/4] / (g a_0)^2,
-// as a function of the initial electric field E_0 (the links at t = 0 fixed).
+// Objectives, over a box of cells after N steps of Simulation.step:
+//   OPX_OBJ_ENERGY: the mean of the per-cell energy density
+//     (EnergyDensity.ComponentComputation, diagnostics/methods/EnergyDensity.java:119-166),
+//     J = mean_x sum_d [E_d^2/2 + |B_d(U) + B_d(Unext)|^2/4] / (g a_0)^2;
+//   OPX_OBJ_ANISOTROPY: the pressure anisotropy P_L / P_T of the projected
+//     energy density components (ProjectedEnergyDensity.java:18-41, 114-179):
+//     per cell and direction j, eps_j = [E_j^2/2 + (|B_j(U)|^2 + |B_j(Unext)|^2)/4] / (g a_j)^2,
+//     eps_L = eps_l (l the longitudinal direction), eps_T = the other two,
+//     P_L = eps_T - eps_L, P_T = eps_L, J = sum_box P_L / sum_box P_T.
+// Inputs: the initial electric field E_0 (the links at t = 0 fixed), or the
+// colour-charge density rho through Gauss's law: the initial E is the
+// projection of the handle's E onto div E = rho (Grid.getGaussConstraint),
+// E_0(rho) = E + divT K^+ (rho - div E) with K = div divT, so a change d of rho
+// moves E_0 by divT K^+ d and dJ/drho = K^+ div (dJ/dE_0).
 //
 // Forward model (FastTYMSolver, physics/fields/FastTYMSolver.java:40-84):
 //     W_0 = exp(-i dt E_0) U                       (initialize: stepLinks)
@@ -281,31 +291,114 @@ __device__ __forceinline__ R energy_cell(const LinkPlanes<SU2<R>, R> &U0, const 
     return en;
 }
 
+struct Obj {
+    int kind;  // OPX_OBJ_ENERGY or OPX_OBJ_ANISOTROPY
+    int dir;   // longitudinal direction of the anisotropy
+    Box box;
+};
+
+// The per-cell terms of the objective: (a, b) = (energy density, 0) or (P_L, P_T)
 template <typename R>
-__global__ void k_energy_box(const R *__restrict__ Wm, const R *__restrict__ Wn, const R *__restrict__ En, Lat L,
-                             Box bx, double *__restrict__ part) {
+__device__ __forceinline__ void obj_cell(const LinkPlanes<SU2<R>, R> &U0, const LinkPlanes<SU2<R>, R> &U1,
+                                         const AlgPlanes<3, R> &E, const Lat &L, long s, const Nbr &nb,
+                                         const Obj &ob, R &a, R &b) {
+    using GG = SU2<R>;
+    if (ob.kind == OPX_OBJ_ENERGY) {
+        a = energy_cell<R>(U0, U1, E, L, s, nb);
+        b = R(0.0);
+        return;
+    }
+    R eL = R(0.0), eT = R(0.0);
+    for (int d = 0; d < 3; d++) {
+        R e[3], b0[3], b1[3];
+        E.load_ro(d, s, e);
+        field_b<GG, R>(U0, L, s, nb, d, b0);
+        field_b<GG, R>(U1, L, s, nb, d, b1);
+        R e2 = R(0.0), bb = R(0.0);
+        for (int q = 0; q < 3; q++) {
+            e2 += e[q] * e[q];
+            bb += b0[q] * b0[q] + b1[q] * b1[q];
+        }
+        const R t = (R(0.5) * e2 + R(0.25) * bb) * R(1.0 / ((L.g * L.a[d]) * (L.g * L.a[d])));
+        if (d == ob.dir) eL += t; else eT += t;
+    }
+    a = eT - eL;
+    b = eL;
+}
+
+// Box sums of a and b: values and (dual numbers) tangents
+template <typename R>
+__global__ void k_obj_box(const R *__restrict__ Wm, const R *__restrict__ Wn, const R *__restrict__ En, Lat L,
+                          Obj ob, double *__restrict__ part) {
     const LinkPlanes<SU2<R>, R> U0{const_cast<R *>(Wm), L.V}, U1{const_cast<R *>(Wn), L.V};
     const AlgPlanes<3, R> E{const_cast<R *>(En), L.V};
-    KSum acc[2] = {{0.0, 0.0}, {0.0, 0.0}};
+    KSum acc[4] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
     for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < L.V; s += (long)gridDim.x * blockDim.x) {
         int x[3];
         site_coords(L, s, x);
-        if (!in_box(x, bx.lo, bx.hi)) continue;
+        if (!in_box(x, ob.box.lo, ob.box.hi)) continue;
         const Nbr nb = neighbours(L, s, x);
-        const R en = energy_cell<R>(U0, U1, E, L, s, nb);
-        two_sum_add(acc[0], value_of(en));
-        two_sum_add(acc[1], tangent_of(en));
+        R a, b;
+        obj_cell<R>(U0, U1, E, L, s, nb, ob, a, b);
+        two_sum_add(acc[0], value_of(a));
+        two_sum_add(acc[1], tangent_of(a));
+        two_sum_add(acc[2], value_of(b));
+        two_sum_add(acc[3], tangent_of(b));
     }
     int q;
-    KSum v = block_reduce<2>(acc, q);
-    if (q >= 0) { part[2 * (blockIdx.x * 2 + q)] = v.s; part[2 * (blockIdx.x * 2 + q) + 1] = v.c; }
+    KSum v = block_reduce<4>(acc, q);
+    if (q >= 0) { part[2 * (blockIdx.x * 4 + q)] = v.s; part[2 * (blockIdx.x * 4 + q) + 1] = v.c; }
 }
 
-__global__ void k_energy_box_final(const double *__restrict__ part, int nb, double inv_n, double *__restrict__ out) {
-    if (threadIdx.x >= 2) return;
+__global__ void k_obj_box_final(const double *__restrict__ part, int nb, double *__restrict__ out) {
+    if (threadIdx.x >= 4) return;
     KSum v{0.0, 0.0};
-    for (int b = 0; b < nb; b++) ksum_merge(v, KSum{part[2 * (b * 2 + threadIdx.x)], part[2 * (b * 2 + threadIdx.x) + 1]});
-    out[threadIdx.x] = (v.s + v.c) * inv_n;
+    for (int b = 0; b < nb; b++) ksum_merge(v, KSum{part[2 * (b * 4 + threadIdx.x)], part[2 * (b * 4 + threadIdx.x) + 1]});
+    out[threadIdx.x] = v.s + v.c;
+}
+
+// Cotangents of the anisotropy J = A / B with respect to E_N, W_{N-1} and W_N:
+// dJ = (dA - J dB) / B, i.e. per direction the weight wT = 1/B (transverse) or
+// wL = (-1 - J)/B (longitudinal) on d eps_j.
+__global__ void k_adj_aniso(const double *__restrict__ Wm, const double *__restrict__ Wn,
+                            const double *__restrict__ En, Lat L, Obj ob, double wT, double wL,
+                            double *__restrict__ Wm_b, double *__restrict__ Wn_b, double *__restrict__ En_b) {
+    const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.V) return;
+    int x[3];
+    site_coords(L, s, x);
+    const AlgPlanes<3, double> E{const_cast<double *>(En), L.V}, Eb{En_b, L.V};
+    if (!in_box(x, ob.box.lo, ob.box.hi)) {
+        const double z[3] = {0, 0, 0};
+        for (int d = 0; d < 3; d++) Eb.store(d, s, z);
+        return;
+    }
+    const Nbr nb = neighbours(L, s, x);
+    const LinkPlanes<G2, double> U0{const_cast<double *>(Wm), L.V}, U1{const_cast<double *>(Wn), L.V};
+    for (int d = 0; d < 3; d++) {
+        const double w = (d == ob.dir ? wL : wT) / ((L.g * L.a[d]) * (L.g * L.a[d]));
+        double e[3], eb[3];
+        E.load_ro(d, s, e);
+        for (int a = 0; a < 3; a++) eb[a] = w * e[a];
+        Eb.store(d, s, eb);
+        const int j = (d + 1) % 3, k = (d + 2) % 3;
+        const double f = L.a[d] / (L.a[j] * L.a[k]);
+        for (int t = 0; t < 2; t++) {
+            const LinkPlanes<G2, double> &Ut = t ? U1 : U0;
+            double *Wb = t ? Wn_b : Wm_b;
+            double bt[3];
+            field_b<G2, double>(Ut, L, s, nb, d, bt);
+            // d(w |B_t|^2 / 4)/dB_t = w B_t / 2; B = 2 f vec(P)
+            Q Pb{{0.0, 0.0, 0.0, 0.0}};
+            for (int a = 0; a < 3; a++) Pb.e[1 + a] = 2 * f * 0.5 * bt[a] * w;
+            const Q A1 = Ut.load(j, s), A2 = Ut.load(k, nb.fwd[j]), A3 = Ut.load(j, nb.fwd[k]), A4 = Ut.load(k, s);
+            const Q A3s = qadj(A3), A4s = qadj(A4);
+            atomic_add_link(Wb, L.V, j, s, qmul(Pb, qadj(qmul(qmul(A2, A3s), A4s))));
+            atomic_add_link(Wb, L.V, k, nb.fwd[j], qmul(qmul(qadj(A1), Pb), qadj(qmul(A3s, A4s))));
+            atomic_add_link(Wb, L.V, j, nb.fwd[k], qadj(qmul(qmul(qmul(qadj(A2), qadj(A1)), Pb), A4)));
+            atomic_add_link(Wb, L.V, k, s, qadj(qmul(qadj(qmul(qmul(A1, A2), A3s)), Pb)));
+        }
+    }
 }
 
 template <int NC, typename R, bool REUNIT>
@@ -355,22 +448,24 @@ struct DevBuf {
     ~DevBuf() { for (void *p : ptrs) cudaFree(p); }
 };
 
-struct AdjArgs {
-    Box box;
+struct ObjArgs {
+    Obj ob;
     int ok;
 };
 
-AdjArgs make_box(const Ctx &c, const int *lo, const int *hi) {
-    AdjArgs a{};
-    a.ok = 1;
+ObjArgs make_obj(const Ctx &c, int kind, int dir, const int *lo, const int *hi) {
+    ObjArgs a{};
+    a.ok = (kind == OPX_OBJ_ENERGY || kind == OPX_OBJ_ANISOTROPY) && (kind == OPX_OBJ_ENERGY || (dir >= 0 && dir < 3));
+    a.ob.kind = kind;
+    a.ob.dir = dir;
     long n = 1;
     for (int i = 0; i < 3; i++) {
-        a.box.lo[i] = lo ? lo[i] : 0;
-        a.box.hi[i] = hi ? hi[i] : c.L.n[i] - 1;
-        if (a.box.lo[i] < 0 || a.box.hi[i] >= c.L.n[i] || a.box.lo[i] > a.box.hi[i]) a.ok = 0;
-        n *= (a.box.hi[i] - a.box.lo[i] + 1);
+        a.ob.box.lo[i] = lo ? lo[i] : 0;
+        a.ob.box.hi[i] = hi ? hi[i] : c.L.n[i] - 1;
+        if (a.ob.box.lo[i] < 0 || a.ob.box.hi[i] >= c.L.n[i] || a.ob.box.lo[i] > a.ob.box.hi[i]) a.ok = 0;
+        n *= (a.ob.box.hi[i] - a.ob.box.lo[i] + 1);
     }
-    a.box.inv_n = 1.0 / (double)n;
+    a.ob.box.inv_n = 1.0 / (double)n;
     return a;
 }
 
@@ -387,17 +482,25 @@ void widen_state(Ctx &c, double *U64, double *E64) {
     }
 }
 
+// J (and with dual numbers dJ) of the objective on (W_{N-1}, W_N, E_N); *A_B
+// receives the box sums (A, B) of the values
 template <typename R>
-double energy_box(Ctx &c, const R *Wm, const R *Wn, const R *E, const Box &bx, double *part, double *out2, double *dJ) {
+double objective_value(Ctx &c, const R *Wm, const R *Wn, const R *E, const Obj &ob, double *part, double *out4,
+                       double *dJ, double *A_B = nullptr) {
     const int nb = 304;
-    k_energy_box<R><<<nb, 256, 0, c.stream>>>(Wm, Wn, E, c.L, bx, part);
-    k_energy_box_final<<<1, 32, 0, c.stream>>>(part, nb, bx.inv_n, out2);
+    k_obj_box<R><<<nb, 256, 0, c.stream>>>(Wm, Wn, E, c.L, ob, part);
+    k_obj_box_final<<<1, 32, 0, c.stream>>>(part, nb, out4);
     c.launches += 2;
-    double h[2] = {0, 0};
-    cudaMemcpyAsync(h, out2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    double h[4] = {0, 0, 0, 0};
+    cudaMemcpyAsync(h, out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
     cudaStreamSynchronize(c.stream);
-    if (dJ) *dJ = h[1];
-    return h[0];
+    if (A_B) { A_B[0] = h[0]; A_B[1] = h[2]; }
+    if (ob.kind == OPX_OBJ_ENERGY) {
+        if (dJ) *dJ = h[1] * ob.box.inv_n;
+        return h[0] * ob.box.inv_n;
+    }
+    if (dJ) *dJ = (h[1] * h[2] - h[0] * h[3]) / (h[2] * h[2]);
+    return h[0] / h[2];
 }
 
 template <typename R>
@@ -425,83 +528,89 @@ int finish(Ctx &c, const char *where) {
     return OPX_OK;
 }
 
-}  // namespace
+// host [V][3][3] (link, direction, component) <-> device planes [3][3][V]
+void to_planes(const double *h, long V, double *t) {
+    for (long s = 0; s < V; s++)
+        for (int d = 0; d < 3; d++)
+            for (int a = 0; a < 3; a++) t[(d * 3 + a) * V + s] = h[(s * 3 + d) * 3 + a];
+}
 
-extern "C" {
+// The initial-E direction of an input direction: dE (host, [V][3][3] or NULL)
+// plus divT K^+ drho (host, [V][3] or NULL), into dev (planes); U64 the
+// handle's links in FP64.  Returns OPX_OK or an error status.
+int input_direction(Ctx &c, const double *U64, const double *dE, const double *drho, double *dev, const char *where) {
+    const long V = c.L.V, nE = V * 9, nr = V * 3;
+    std::vector<double> t(nE, 0.0);
+    if (dE) to_planes(dE, V, t.data());
+    cudaMemcpyAsync(dev, t.data(), nE * 8, cudaMemcpyHostToDevice, c.stream);
+    cudaStreamSynchronize(c.stream);
+    if (!drho) return OPX_OK;
+    DevBuf B;
+    double *r = B.get<double>(nr), *mu = B.get<double>(nr);
+    if (!B.ok) { c.err = std::string(where) + ": out of device memory"; return OPX_ERR_NOMEM; }
+    std::vector<double> tr(nr);
+    for (long s = 0; s < V; s++)
+        for (int a = 0; a < 3; a++) tr[a * V + s] = drho[s * 3 + a];
+    cudaMemcpyAsync(r, tr.data(), nr * 8, cudaMemcpyHostToDevice, c.stream);
+    int rc = ic_covariant_solve(c, U64, r, mu, 1e-13, 20000, nullptr);
+    if (rc) { c.err = std::string(where) + ": " + c.err; return rc; }
+    ic_divT(c, U64, mu, dev, 1);
+    return OPX_OK;
+}
 
-int opx_energy_objective(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double h,
-                         double *J) {
-    if (!ctx || !J) return OPX_ERR_INVALID;
-    Ctx &c = ctx_of(ctx);
-    int rc = check_su2(c, nsteps, "opx_energy_objective");
-    if (rc) return rc;
-    AdjArgs ar = make_box(c, lo, hi);
-    if (!ar.ok) { c.err = "opx_energy_objective: box outside the lattice"; return OPX_ERR_INVALID; }
+int objective_value_impl(Ctx &c, const ObjArgs &ar, int nsteps, const double *dE, const double *drho, double h,
+                         double *J, const char *where) {
     const long V = c.L.V, nU = link_elems(V, 4), nE = V * 9;
     DevBuf B;
     double *U0 = B.get<double>(nU), *Wa = B.get<double>(nU), *Wb = B.get<double>(nU), *E = B.get<double>(nE);
-    double *dEd = B.get<double>(nE), *part = B.get<double>(4 * 304), *out2 = B.get<double>(2);
-    if (!B.ok) { c.err = "opx_energy_objective: out of device memory"; return OPX_ERR_NOMEM; }
+    double *dEd = B.get<double>(nE), *part = B.get<double>(8 * 304), *out4 = B.get<double>(4);
+    if (!B.ok) { c.err = std::string(where) + ": out of device memory"; return OPX_ERR_NOMEM; }
     widen_state(c, U0, E);
-    if (dE && h != 0.0) {
-        // host [V][3][3] -> planes [3][3][V]
-        std::vector<double> t(nE);
-        for (long s = 0; s < V; s++)
-            for (int d = 0; d < 3; d++)
-                for (int a = 0; a < 3; a++) t[(d * 3 + a) * V + s] = dE[(s * 3 + d) * 3 + a];
-        cudaMemcpyAsync(dEd, t.data(), nE * 8, cudaMemcpyHostToDevice, c.stream);
+    if ((dE || drho) && h != 0.0) {
+        int rc = input_direction(c, U0, dE, drho, dEd, where);
+        if (rc) return rc;
         k_axpy_d<<<grid_for(nE, 256), 256, 0, c.stream>>>(E, dEd, h, nE);
-        cudaStreamSynchronize(c.stream);
+        c.launches++;
     }
     k_links_plain<2, double><<<grid_for(V, 128), 128, 0, c.stream>>>(U0, E, Wa, c.L);
+    c.launches++;
     double *last, *prev;
     fwd_steps<double>(c, Wa, Wb, E, nsteps, &last, &prev);
-    *J = energy_box<double>(c, prev, last, E, ar.box, part, out2, nullptr);
-    return finish(c, "opx_energy_objective");
+    *J = objective_value<double>(c, prev, last, E, ar.ob, part, out4, nullptr);
+    return finish(c, where);
 }
 
-int opx_energy_tangent(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double *J,
-                       double *dJ) {
-    if (!ctx || !J || !dJ || !dE) return OPX_ERR_INVALID;
-    Ctx &c = ctx_of(ctx);
-    int rc = check_su2(c, nsteps, "opx_energy_tangent");
-    if (rc) return rc;
-    AdjArgs ar = make_box(c, lo, hi);
-    if (!ar.ok) { c.err = "opx_energy_tangent: box outside the lattice"; return OPX_ERR_INVALID; }
+int objective_tangent_impl(Ctx &c, const ObjArgs &ar, int nsteps, const double *dE, const double *drho, double *J,
+                           double *dJ, const char *where) {
     const long V = c.L.V, nU = link_elems(V, 4), nE = V * 9;
     DevBuf B;
     double *U0 = B.get<double>(nU), *E0 = B.get<double>(nE), *dEd = B.get<double>(nE);
     Dual *Ud = B.get<Dual>(nU), *Wa = B.get<Dual>(nU), *Wb = B.get<Dual>(nU), *Ed = B.get<Dual>(nE);
-    double *part = B.get<double>(4 * 304), *out2 = B.get<double>(2);
-    if (!B.ok) { c.err = "opx_energy_tangent: out of device memory"; return OPX_ERR_NOMEM; }
+    double *part = B.get<double>(8 * 304), *out4 = B.get<double>(4);
+    if (!B.ok) { c.err = std::string(where) + ": out of device memory"; return OPX_ERR_NOMEM; }
     widen_state(c, U0, E0);
-    std::vector<double> t(nE);
-    for (long s = 0; s < V; s++)
-        for (int d = 0; d < 3; d++)
-            for (int a = 0; a < 3; a++) t[(d * 3 + a) * V + s] = dE[(s * 3 + d) * 3 + a];
-    cudaMemcpyAsync(dEd, t.data(), nE * 8, cudaMemcpyHostToDevice, c.stream);
+    int rc = input_direction(c, U0, dE, drho, dEd, where);
+    if (rc) return rc;
     k_make_dual<<<grid_for(nU, 256), 256, 0, c.stream>>>(U0, nullptr, Ud, nU);
     k_make_dual<<<grid_for(nE, 256), 256, 0, c.stream>>>(E0, dEd, Ed, nE);
     k_links_plain<2, Dual><<<grid_for(V, 128), 128, 0, c.stream>>>(Ud, Ed, Wa, c.L);
     c.launches += 3;
     Dual *last, *prev;
     fwd_steps<Dual>(c, Wa, Wb, Ed, nsteps, &last, &prev);
-    *J = energy_box<Dual>(c, prev, last, Ed, ar.box, part, out2, dJ);
-    cudaStreamSynchronize(c.stream);
-    return finish(c, "opx_energy_tangent");
+    *J = objective_value<Dual>(c, prev, last, Ed, ar.ob, part, out4, dJ);
+    return finish(c, where);
 }
 
-int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const int *hi, double *J, double *grad,
-                        size_t count) {
-    if (!ctx || !J || !grad) return OPX_ERR_INVALID;
-    Ctx &c = ctx_of(ctx);
-    int rc = check_su2(c, nsteps, "opx_energy_gradient");
-    if (rc) return rc;
-    if (ckpt < 1) { c.err = "opx_energy_gradient: ckpt must be >= 1"; return OPX_ERR_INVALID; }
+int objective_gradient_impl(Ctx &c, const ObjArgs &ar, int nsteps, int ckpt, int wrt, double *J, double *grad,
+                            size_t count, const char *where) {
     const long V = c.L.V, nU = link_elems(V, 4), nE = V * 9;
-    if (count != (size_t)nE) { c.err = "opx_energy_gradient: gradient must hold V*3*3 doubles"; return OPX_ERR_INVALID; }
-    AdjArgs ar = make_box(c, lo, hi);
-    if (!ar.ok) { c.err = "opx_energy_gradient: box outside the lattice"; return OPX_ERR_INVALID; }
+    if (ckpt < 1) { c.err = std::string(where) + ": ckpt must be >= 1"; return OPX_ERR_INVALID; }
+    if (wrt != OPX_WRT_E && wrt != OPX_WRT_RHO) { c.err = std::string(where) + ": unknown input"; return OPX_ERR_INVALID; }
+    const size_t want = wrt == OPX_WRT_E ? (size_t)nE : (size_t)V * 3;
+    if (count != want) {
+        c.err = std::string(where) + (wrt == OPX_WRT_E ? ": gradient must hold V*3*3 doubles" : ": gradient must hold V*3 doubles");
+        return OPX_ERR_INVALID;
+    }
     const int nseg = (nsteps + ckpt - 1) / ckpt;
     const int rs = c.prec == OPX_F64 ? 8 : 4;
     DevBuf B;
@@ -514,8 +623,8 @@ int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const
     for (int m = 0; m <= ckpt; m++) { segW[m] = B.get<double>(nU); segE[m] = B.get<double>(nE); }
     double *Wbar[2] = {B.get<double>(nU), B.get<double>(nU)}, *Ebar[2] = {B.get<double>(nE), B.get<double>(nE)};
     double *Wm_b = B.get<double>(nU), *Sbar = B.get<double>(nU), *Uown = B.get<double>(nU);
-    double *part = B.get<double>(4 * 304), *out2 = B.get<double>(2);
-    if (!B.ok) { c.err = "opx_energy_gradient: out of device memory"; return OPX_ERR_NOMEM; }
+    double *part = B.get<double>(8 * 304), *out4 = B.get<double>(4);
+    if (!B.ok) { c.err = std::string(where) + ": out of device memory"; return OPX_ERR_NOMEM; }
     cudaMemcpyAsync(Ur0, c.U, nU * rs, cudaMemcpyDeviceToDevice, c.stream);
     cudaMemcpyAsync(Er, c.E, nE * rs, cudaMemcpyDeviceToDevice, c.stream);
     widen_state(c, U64, E64);
@@ -557,11 +666,18 @@ int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const
             c.launches++;
         }
         if (k == nseg - 1) {
-            Jv = energy_box<double>(c, segW[len - 1], segW[len], segE[len], ar.box, part, out2, nullptr);
+            double AB[2];
+            Jv = objective_value<double>(c, segW[len - 1], segW[len], segE[len], ar.ob, part, out4, nullptr, AB);
             cudaMemsetAsync(Wm_b, 0, nU * 8, c.stream);
             cudaMemsetAsync(Wbar[wb], 0, nU * 8, c.stream);
-            k_adj_objective<<<gs, 128, 0, c.stream>>>(segW[len - 1], segW[len], segE[len], c.L, ar.box, Wm_b,
+            if (ar.ob.kind == OPX_OBJ_ENERGY) {
+                k_adj_objective<<<gs, 128, 0, c.stream>>>(segW[len - 1], segW[len], segE[len], c.L, ar.ob.box, Wm_b,
+                                                          Wbar[wb], Ebar[wb]);
+            } else {
+                const double wT = 1.0 / AB[1], wL = (-1.0 - Jv) / AB[1];
+                k_adj_aniso<<<gs, 128, 0, c.stream>>>(segW[len - 1], segW[len], segE[len], c.L, ar.ob, wT, wL, Wm_b,
                                                       Wbar[wb], Ebar[wb]);
+            }
             c.launches++;
         }
         for (int m = len; m >= 1; m--) {
@@ -580,15 +696,101 @@ int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const
     // W_0 = exp(-i dt E_0) U
     k_adj_init_links<<<gs, 128, 0, c.stream>>>(U64, E64, Wbar[wb], c.L, Ebar[wb]);
     c.launches++;
-    std::vector<double> t(nE);
-    cudaMemcpyAsync(t.data(), Ebar[wb], nE * 8, cudaMemcpyDeviceToHost, c.stream);
-    rc = finish(c, "opx_energy_gradient");
+    int rc = finish(c, where);
     if (rc) return rc;
-    for (long s = 0; s < V; s++)
-        for (int d = 0; d < 3; d++)
-            for (int a = 0; a < 3; a++) grad[(s * 3 + d) * 3 + a] = t[(d * 3 + a) * V + s];
+    if (wrt == OPX_WRT_E) {
+        std::vector<double> t(nE);
+        cudaMemcpyAsync(t.data(), Ebar[wb], nE * 8, cudaMemcpyDeviceToHost, c.stream);
+        rc = finish(c, where);
+        if (rc) return rc;
+        for (long s = 0; s < V; s++)
+            for (int d = 0; d < 3; d++)
+                for (int a = 0; a < 3; a++) grad[(s * 3 + d) * 3 + a] = t[(d * 3 + a) * V + s];
+    } else {
+        // dJ/drho = K^+ div (dJ/dE_0)
+        double *r = Sbar, *nu = Uown;  // site fields ([3][V]) in the free cotangent buffers
+        ic_div(c, U64, Ebar[wb], r);
+        rc = ic_covariant_solve(c, U64, r, nu, 1e-13, 20000, nullptr);
+        if (rc) { c.err = std::string(where) + ": " + c.err; return rc; }
+        std::vector<double> t(V * 3);
+        cudaMemcpyAsync(t.data(), nu, V * 3 * 8, cudaMemcpyDeviceToHost, c.stream);
+        rc = finish(c, where);
+        if (rc) return rc;
+        for (long s = 0; s < V; s++)
+            for (int a = 0; a < 3; a++) grad[s * 3 + a] = t[a * V + s];
+    }
     *J = Jv;
     return OPX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int opx_objective_value(opx_ctx *ctx, const opx_objective *obj, int nsteps, const double *dE, const double *drho,
+                        double h, double *J) {
+    if (!ctx || !obj || !J) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_objective_value");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, obj->kind, obj->direction, obj->lo, obj->hi);
+    if (!ar.ok) { c.err = "opx_objective_value: unknown objective or box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_value_impl(c, ar, nsteps, dE, drho, h, J, "opx_objective_value");
+}
+
+int opx_objective_tangent(opx_ctx *ctx, const opx_objective *obj, int nsteps, const double *dE, const double *drho,
+                          double *J, double *dJ) {
+    if (!ctx || !obj || !J || !dJ || (!dE && !drho)) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_objective_tangent");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, obj->kind, obj->direction, obj->lo, obj->hi);
+    if (!ar.ok) { c.err = "opx_objective_tangent: unknown objective or box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_tangent_impl(c, ar, nsteps, dE, drho, J, dJ, "opx_objective_tangent");
+}
+
+int opx_objective_gradient(opx_ctx *ctx, const opx_objective *obj, int nsteps, int ckpt, int wrt, double *J,
+                           double *grad, size_t count) {
+    if (!ctx || !obj || !J || !grad) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_objective_gradient");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, obj->kind, obj->direction, obj->lo, obj->hi);
+    if (!ar.ok) { c.err = "opx_objective_gradient: unknown objective or box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_gradient_impl(c, ar, nsteps, ckpt, wrt, J, grad, count, "opx_objective_gradient");
+}
+
+int opx_energy_objective(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double h,
+                         double *J) {
+    if (!ctx || !J) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_energy_objective");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, OPX_OBJ_ENERGY, 0, lo, hi);
+    if (!ar.ok) { c.err = "opx_energy_objective: box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_value_impl(c, ar, nsteps, dE, nullptr, h, J, "opx_energy_objective");
+}
+
+int opx_energy_tangent(opx_ctx *ctx, int nsteps, const int *lo, const int *hi, const double *dE, double *J,
+                       double *dJ) {
+    if (!ctx || !J || !dJ || !dE) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_energy_tangent");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, OPX_OBJ_ENERGY, 0, lo, hi);
+    if (!ar.ok) { c.err = "opx_energy_tangent: box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_tangent_impl(c, ar, nsteps, dE, nullptr, J, dJ, "opx_energy_tangent");
+}
+
+int opx_energy_gradient(opx_ctx *ctx, int nsteps, int ckpt, const int *lo, const int *hi, double *J, double *grad,
+                        size_t count) {
+    if (!ctx || !J || !grad) return OPX_ERR_INVALID;
+    Ctx &c = ctx_of(ctx);
+    int rc = check_su2(c, nsteps, "opx_energy_gradient");
+    if (rc) return rc;
+    ObjArgs ar = make_obj(c, OPX_OBJ_ENERGY, 0, lo, hi);
+    if (!ar.ok) { c.err = "opx_energy_gradient: box outside the lattice"; return OPX_ERR_INVALID; }
+    return objective_gradient_impl(c, ar, nsteps, ckpt, OPX_WRT_E, J, grad, count, "opx_energy_gradient");
 }
 
 }  // extern "C"

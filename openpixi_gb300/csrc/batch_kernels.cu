@@ -26,6 +26,7 @@
 #include "ksum.cuh"
 #include "leapfrog.cuh"
 #include "observables.cuh"
+#include "su3_pair.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -66,6 +67,49 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BEvent<R> *__res
         }
         cluster.sync();
     }
+}
+
+// SU(3) FP32: the paired form of the single-lattice kernel (two sites per
+// thread in paired FP32 instructions, su3_pair.cuh).  Thread slot t of an
+// event covers sites sa = 64 (t / 32) + t % 32 and sb = sa + 32.
+template <typename I>
+__global__ void __launch_bounds__(128, 3) k_batch_persistent_su3f(const BEvent<float> *__restrict__ ev,
+                                                                  const int *__restrict__ list,
+                                                                  const int *__restrict__ begin, int nsteps,
+                                                                  int cur, long step0, int reunit_every) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned csize = cluster.num_blocks();
+    const unsigned rank = cluster.block_rank();
+    const int cid = blockIdx.x / csize;
+    const int e0 = begin[cid], e1 = begin[cid + 1];
+    const I first = (I)rank * (I)blockDim.x + (I)threadIdx.x;
+    const I stride = (I)csize * (I)blockDim.x;
+    for (int k = 0; k < nsteps; k++) {
+        const bool reunit = reunit_every > 0 && ((step0 + k + 1) % reunit_every) == 0;
+        const int rd = cur ^ ((k + 1) & 1), wr = cur ^ (k & 1);
+        for (int q = e0; q < e1; q++) {
+            const BEvent<float> &e = ev[list[q]];
+            const float *U = e.B[rd];
+            float *Un = e.B[wr];
+            const I V = (I)e.L.V, slots = ((V + 63) >> 6) << 5;
+            for (I t = first; t < slots; t += stride) {
+                const I sa = ((t >> 5) << 6) + (t & 31);
+                if (sa >= V) continue;
+                I sb = sa + 32;
+                const bool vb = sb < V;
+                if (!vb) sb = sa;
+                if (reunit) update_site_pair<I, false, true>(U, e.E, nullptr, Un, e.L, sa, sb, true, vb);
+                else update_site_pair<I, false, false>(U, e.E, nullptr, Un, e.L, sa, sb, true, vb);
+            }
+        }
+        cluster.sync();
+    }
+}
+
+// the persistent kernel of a batch's group and precision
+template <int NC, typename R, typename I> static void *persistent_kernel() {
+    if constexpr (NC == 3 && sizeof(R) == 4) return (void *)k_batch_persistent_su3f<I>;
+    else return (void *)k_batch_persistent<NC, R, I>;
 }
 
 template <int NC, typename R>
@@ -220,13 +264,13 @@ static cudaError_t launch_persistent(Batch &b, int nsteps, cudaStream_t st) {
     cfg.numAttrs = 1;
     b.launches++;
     const long step0 = b.reunit_every > 0 ? b.steps % b.reunit_every : 0L;
-    if (b.int_offsets)
-        return cudaLaunchKernelEx(&cfg, k_batch_persistent<NC, R, int>, (const BEvent<R> *)b.ev_dev,
-                                  (const int *)b.list_dev, (const int *)b.begin_dev, nsteps, b.cur, step0,
-                                  b.reunit_every);
-    return cudaLaunchKernelEx(&cfg, k_batch_persistent<NC, R, long>, (const BEvent<R> *)b.ev_dev,
-                              (const int *)b.list_dev, (const int *)b.begin_dev, nsteps, b.cur, step0,
-                              b.reunit_every);
+    const BEvent<R> *ev = (const BEvent<R> *)b.ev_dev;
+    const int *list = (const int *)b.list_dev, *begin = (const int *)b.begin_dev;
+    const int cur = b.cur, re = b.reunit_every;
+    void *args[] = {(void *)&ev, (void *)&list, (void *)&begin, (void *)&nsteps, (void *)&cur, (void *)&step0,
+                    (void *)&re};
+    void *k = b.int_offsets ? persistent_kernel<NC, R, int>() : persistent_kernel<NC, R, long>();
+    return cudaLaunchKernelExC(&cfg, k, args);
 }
 
 template <int NC, typename R>
@@ -242,7 +286,7 @@ static int max_clusters(Batch &b, int cluster, int block) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    void *k = b.int_offsets ? (void *)k_batch_persistent<NC, R, int> : (void *)k_batch_persistent<NC, R, long>;
+    void *k = b.int_offsets ? persistent_kernel<NC, R, int>() : persistent_kernel<NC, R, long>();
     if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;

@@ -108,91 +108,138 @@ __device__ void ref_su2_act(const double *v, const double *u, double *out) {
     out[2] = 2 * r[3];
 }
 
-__device__ __forceinline__ long cpic_cell(const Lat &L, const int *c) {
-    long idx = 0;
-    for (int i = 0; i < 3; i++) {
-        long r = ((long)c[i] % L.n[i] + L.n[i]) % L.n[i];
-        idx = i == 0 ? r : idx * L.n[i] + r;
-    }
-    return idx;
+// Grid.getCellIndex with the periodic wrap (physics/grid/Grid.java:779-786)
+__device__ __forceinline__ int cpic_cell(const Lat &L, int c0, int c1, int c2) {
+    int r0 = c0 % L.n[0], r1 = c1 % L.n[1], r2 = c2 % L.n[2];
+    r0 += r0 < 0 ? L.n[0] : 0;
+    r1 += r1 < 0 ? L.n[1] : 0;
+    r2 += r2 < 0 ? L.n[2] : 0;
+    return (r0 * L.n[1] + r1) * L.n[2] + r2;
 }
 
+// (int) Math.rint(p / a) (GridFunctions.nearestGridPoint, physics/util/GridFunctions.java:67-73)
+// with the correctly rounded quotient, dividing only where it can matter.  For
+// a = 1 the quotient is p.  Otherwise q = p * (1/a) is within 3.01 u |q| of the
+// correctly rounded p / a (u = 2^-53: one rounding in 1/a, one in the product,
+// against one in the quotient); rint maps every value strictly between two
+// consecutive half-integers to the same integer, so rint(q) is the reference's
+// result unless a half-integer lies within that distance of q (the fraction
+// itself is formed with an error below u), and then the quotient is formed.
+// GB300's FP64 division is a dozen FP64 instructions at 1/64 of the FP32 rate.
+__device__ __forceinline__ int ngp_index(double p, double a, double inv_a) {
+    if (a == 1.0) return (int)rint(p);
+    const double q = p * inv_a;
+    const double h = fabs((q - floor(q)) - 0.5);
+    if (h > 1e-15 * (fabs(q) + 1.0)) return (int)rint(q);
+    return (int)rint(p / a);
+}
+
+__device__ __forceinline__ int sel3(int a0, int a1, int a2, int d) { return d == 0 ? a0 : (d == 1 ? a1 : a2); }
+__device__ __forceinline__ double sel3(double a0, double a1, double a2, int d) {
+    return d == 0 ? a0 : (d == 1 ? a1 : a2);
+}
+
+// Per-direction constants of the push, formed on the host with the same IEEE
+// divisions the reference makes: 1/a_i, and a_d / dt of the current
+// (CGCParticleInterpolationNGP.java:43,46; (-a)/dt = -(a/dt) exactly).
+struct CpicConst {
+    double inv_a[3], a_dt[3];
+};
+
 template <int NC>
-__global__ void k_cpic_push(Particles P, const double *__restrict__ Unext, Lat L, int reassign) {
+__global__ void __launch_bounds__(256) k_cpic_push(Particles P, const double *__restrict__ Unext, Lat L,
+                                                   CpicConst K, int reassign) {
     constexpr int NG = NC == 3 ? 18 : 4;
     constexpr int NAR = NC == 3 ? 9 : 3;
     const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long n = P.n;
     if (k >= n) return;
+    const double *__restrict__ pin = reassign ? P.pos1 : P.pos0;
+    const double *__restrict__ qa = reassign ? P.q1 : P.q0;
+    const double *__restrict__ qb = reassign ? P.q0 : P.q1;
     double p0[3], p1[3], vel[3], q0[NAR], q1[NAR];
+#pragma unroll
     for (int i = 0; i < 3; i++) {
-        p0[i] = reassign ? P.pos1[i * n + k] : P.pos0[i * n + k];
+        p0[i] = pin[i * n + k];
         vel[i] = P.vel[i * n + k];
     }
+#pragma unroll
     for (int a = 0; a < NAR; a++) {
-        q0[a] = reassign ? P.q1[a * n + k] : P.q0[a * n + k];
-        q1[a] = reassign ? P.q0[a * n + k] : P.q1[a * n + k];
+        q0[a] = qa[a * n + k];
+        q1[a] = qb[a * n + k];
     }
-    // nearest grid points: (int) Math.rint(pos / a) (physics/util/GridFunctions.java:67-73)
-    int o[3], m[3];
-    for (int i = 0; i < 3; i++) o[i] = (int)rint(p0[i] / L.a[i]);
-    const long cell_old = cpic_cell(L, o);
-    P.key_rho[k] = (int)cell_old;
-    for (int a = 0; a < NAR; a++) P.val_rho[a * n + k] = q0[a];
-    for (int i = 0; i < 3; i++) p1[i] = p0[i] + vel[i] * L.dt;
-    for (int i = 0; i < 3; i++) m[i] = (int)rint(p1[i] / L.a[i]);
     const int d = P.dir[k];
+    // nearest grid points before and after the move
+    int o[3], m[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) o[i] = ngp_index(p0[i], L.a[i], K.inv_a[i]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) p1[i] = p0[i] + vel[i] * L.dt;
+#pragma unroll
+    for (int i = 0; i < 3; i++) m[i] = ngp_index(p1[i], L.a[i], K.inv_a[i]);
+    const int cell_old = cpic_cell(L, o[0], o[1], o[2]);
+    P.key_rho[k] = cell_old;
+#pragma unroll
+    for (int a = 0; a < NAR; a++) P.val_rho[a * n + k] = q0[a];
     double Q0n[NAR], Q1n[NAR];
     int keyj = -1;
-    if (o[d] != m[d]) {
-        const long cell_new = cpic_cell(L, m);
+    if (sel3(o[0], o[1], o[2], d) != sel3(m[0], m[1], m[2], d)) {
+        const int cell_new = cpic_cell(L, m[0], m[1], m[2]);
+        const double vd = sel3(vel[0], vel[1], vel[2], d);
         // P.U: Unext(old) for v > 0, Unext(new)^dagger otherwise; the charge
         // update uses U^dagger, i.e. Unext(old)^dagger or Unext(new).
         double Uadj[NG], U[NG];
-        const long cl = P.vel[d * n + k] > 0 ? cell_old : cell_new;
+        const long cl = vd > 0 ? cell_old : cell_new;
+#pragma unroll
         for (int c = 0; c < NG; c++) U[c] = Unext[link_offset(L.V, NG, d, c, cl)];
-        if (vel[d] > 0) {
+        if (vd > 0) {
             if (NC == 3) ref_su3_adj(U, Uadj);
             else { Uadj[0] = U[0]; Uadj[1] = -U[1]; Uadj[2] = -U[2]; Uadj[3] = -U[3]; }
         } else {
             // (U^dagger)^dagger = U exactly
+#pragma unroll
             for (int c = 0; c < NG; c++) Uadj[c] = U[c];
         }
+#pragma unroll
         for (int a = 0; a < NAR; a++) Q0n[a] = q0[a];
         if (NC == 3) ref_su3_act(q0, Uadj, Q1n);
         else ref_su2_act(q0, Uadj, Q1n);
-        if (vel[d] > 0) {
-            const double f = L.a[d] / L.dt;
-            keyj = (int)(cell_old * 3 + d);
+        const double f = sel3(K.a_dt[0], K.a_dt[1], K.a_dt[2], d);
+        if (vd > 0) {
+            keyj = cell_old * 3 + d;
+#pragma unroll
             for (int a = 0; a < NAR; a++) P.val_j[a * n + k] = Q0n[a] * f;
         } else {
-            const double f = -L.a[d] / L.dt;
-            keyj = (int)(cell_new * 3 + d);
-            for (int a = 0; a < NAR; a++) P.val_j[a * n + k] = Q1n[a] * f;
+            keyj = cell_new * 3 + d;
+#pragma unroll
+            for (int a = 0; a < NAR; a++) P.val_j[a * n + k] = Q1n[a] * -f;
         }
     } else {
         // no cell change: Q0 and Q1 swap back (CGCParticleSolver.java:30-35)
+#pragma unroll
         for (int a = 0; a < NAR; a++) { Q0n[a] = q1[a]; Q1n[a] = q0[a]; }
     }
     P.key_j[k] = keyj;
+    // bucket sizes of the counting sort (the buckets are empty on entry)
+    atomicAdd(&P.count[cell_old], 1);
+    if (keyj >= 0) atomicAdd(&P.count[L.V + keyj], 1);
+#pragma unroll
     for (int i = 0; i < 3; i++) { P.pos0[i * n + k] = p0[i]; P.pos1[i * n + k] = p1[i]; }
+#pragma unroll
     for (int a = 0; a < NAR; a++) { P.q0[a * n + k] = Q0n[a]; P.q1[a * n + k] = Q1n[a]; }
 }
 
-__global__ void k_cpic_count(Particles P, long V) {
-    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.n) return;
-    atomicAdd(&P.count[P.key_rho[k]], 1);
-    if (P.key_j[k] >= 0) atomicAdd(&P.count[V + P.key_j[k]], 1);
-}
-
+// Places each particle in its buckets: bucket sizes count down to zero, so
+// they are empty again for the next step, and a bucket's entries fill
+// [offset[key], offset[key + 1]) in some order (the segmented sum restores
+// the particle order).
 __global__ void k_cpic_scatter(Particles P, long V) {
     const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const int kr = P.key_rho[k];
-    P.slots[P.offset[kr] + atomicAdd(&P.cursor[kr], 1)] = (int)k;
+    P.slots[P.offset[kr] + atomicSub(&P.count[kr], 1) - 1] = (int)k;
     const int kj = P.key_j[k];
-    if (kj >= 0) P.slots[P.offset[V + kj] + atomicAdd(&P.cursor[V + kj], 1)] = (int)k;
+    if (kj >= 0) P.slots[P.offset[V + kj] + atomicSub(&P.count[V + kj], 1) - 1] = (int)k;
 }
 
 // one thread per key: keys [0,V) are rho cells, [V, 4V) are (cell*3 + dir) of J
@@ -202,7 +249,7 @@ __global__ void k_cpic_segsum(Particles P, long V, double *__restrict__ rho, dou
     constexpr int NA = NC == 3 ? 8 : 3;
     const long key = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (key >= 4 * V) return;
-    const int beg = P.offset[key], cnt = P.count[key];
+    const int beg = P.offset[key], cnt = P.offset[key + 1] - beg;
     int *seg = P.slots + beg;
     // ascending particle index (buckets hold a handful of entries)
     for (int i = 1; i < cnt; i++) {
@@ -238,48 +285,87 @@ __global__ void k_cpic_segsum(Particles P, long V, double *__restrict__ rho, dou
 }
 
 // ---- exclusive scan of int counts (three phases) ----
-constexpr int SCAN_B = 1024;
-__global__ void k_scan_block(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ sums, long n) {
-    __shared__ int sh[SCAN_B];
-    const long i = (long)blockIdx.x * SCAN_B + threadIdx.x;
-    int v = i < n ? in[i] : 0;
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = 1; o < SCAN_B; o <<= 1) {
-        int t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
-        __syncthreads();
-        sh[threadIdx.x] += t;
-        __syncthreads();
+// A block scans SCAN_B * 4 counts, four per thread: each thread's four, then
+// the threads' totals by warp shuffles and the warps' totals in shared memory.
+constexpr int SCAN_B = 1024, SCAN_PER = 4, SCAN_TILE = SCAN_B * SCAN_PER;
+
+// exclusive prefix of v over the block (all SCAN_B threads take part); total = the block's sum
+__device__ __forceinline__ int block_exclusive_scan(int v, int &total) {
+    __shared__ int warp_tot[SCAN_B / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    if (i < n) out[i] = sh[threadIdx.x] - v;  // exclusive
-    if (threadIdx.x == SCAN_B - 1) sums[blockIdx.x] = sh[SCAN_B - 1];
-}
-__global__ void k_scan_sums(int *__restrict__ sums, long nb) {
-    // single block: exclusive scan of block sums with a running carry
-    __shared__ int sh[SCAN_B];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
+    if (lane == 31) warp_tot[w] = x;
     __syncthreads();
-    for (long base = 0; base < nb; base += SCAN_B) {
-        const long i = base + threadIdx.x;
-        int v = i < nb ? sums[i] : 0;
-        sh[threadIdx.x] = v;
-        __syncthreads();
-        for (int o = 1; o < SCAN_B; o <<= 1) {
-            int t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
-            __syncthreads();
-            sh[threadIdx.x] += t;
-            __syncthreads();
+    if (w == 0) {
+        int t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
         }
-        if (i < nb) sums[i] = carry + sh[threadIdx.x] - v;
-        __syncthreads();
-        if (threadIdx.x == SCAN_B - 1) carry += sh[SCAN_B - 1];
-        __syncthreads();
+        warp_tot[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    total = warp_tot[SCAN_B / 32 - 1];
+    const int before = w > 0 ? warp_tot[w - 1] : 0;
+    __syncthreads();  // warp_tot is reused by the next call
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_B) k_scan_block(const int *__restrict__ in, int *__restrict__ out,
+                                                       int *__restrict__ sums, long n) {
+    const long base = (long)blockIdx.x * SCAN_TILE + (long)threadIdx.x * SCAN_PER;
+    int v[SCAN_PER], t = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_PER; j++) {
+        v[j] = base + j < n ? in[base + j] : 0;
+        t += v[j];
+    }
+    int total;
+    int run = block_exclusive_scan(t, total);
+#pragma unroll
+    for (int j = 0; j < SCAN_PER; j++) {
+        if (base + j < n) out[base + j] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the block sums, in chunks of SCAN_TILE with a carry
+__global__ void __launch_bounds__(SCAN_B) k_scan_sums(int *__restrict__ sums, long nb) {
+    int carry = 0;
+    for (long chunk = 0; chunk < nb; chunk += SCAN_TILE) {
+        const long base = chunk + (long)threadIdx.x * SCAN_PER;
+        int v[SCAN_PER], t = 0;
+#pragma unroll
+        for (int j = 0; j < SCAN_PER; j++) {
+            v[j] = base + j < nb ? sums[base + j] : 0;
+            t += v[j];
+        }
+        int total;
+        int run = carry + block_exclusive_scan(t, total);
+#pragma unroll
+        for (int j = 0; j < SCAN_PER; j++) {
+            if (base + j < nb) sums[base + j] = run;
+            run += v[j];
+        }
+        carry += total;
     }
 }
-__global__ void k_scan_add(int *__restrict__ out, const int *__restrict__ sums, long n) {
-    const long i = (long)blockIdx.x * SCAN_B + threadIdx.x;
-    if (i < n) out[i] += sums[blockIdx.x];
+
+__global__ void __launch_bounds__(SCAN_B) k_scan_add(int *__restrict__ out, const int *__restrict__ sums, long n) {
+    const int add = sums[blockIdx.x];
+    const long base = (long)blockIdx.x * SCAN_TILE + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < SCAN_PER; j++) {
+        const long i = base + (long)j * SCAN_B;
+        if (i < n) out[i] += add;
+    }
 }
 
 int cpic_alloc(Ctx &c, long n) {
@@ -301,12 +387,13 @@ int cpic_alloc(Ctx &c, long n) {
     al((void **)&P.key_j, sizeof(int) * cap);
     al((void **)&P.val_rho, sizeof(double) * nar * cap);
     al((void **)&P.val_j, sizeof(double) * nar * cap);
-    al((void **)&P.count, sizeof(int) * 4 * V);
-    al((void **)&P.offset, sizeof(int) * 4 * V);
-    al((void **)&P.cursor, sizeof(int) * 4 * V);
+    // bucket sizes (zero between steps) and their exclusive scan over 4V + 1 keys
+    al((void **)&P.count, sizeof(int) * (4 * V + 1));
+    al((void **)&P.offset, sizeof(int) * (4 * V + 1));
     al((void **)&P.slots, sizeof(int) * 2 * cap);
-    P.scan_tmp_len = (4 * V + SCAN_B - 1) / SCAN_B;
+    P.scan_tmp_len = (4 * V + 1 + SCAN_TILE - 1) / SCAN_TILE;
     al((void **)&P.scan_tmp, sizeof(int) * P.scan_tmp_len);
+    if (ok && cudaMemset(P.count, 0, sizeof(int) * (4 * V + 1)) != cudaSuccess) ok = false;
     if (!ok) { cpic_free(c); c.err = "particle buffers: out of device memory"; return OPX_ERR_NOMEM; }
     P.cap = cap;
     P.n = n;
@@ -316,7 +403,7 @@ int cpic_alloc(Ctx &c, long n) {
 void cpic_free(Ctx &c) {
     Particles &P = c.P;
     void *ptrs[] = {P.pos0, P.pos1, P.vel, P.q0, P.q1, P.dir, P.key_rho, P.key_j, P.val_rho,
-                    P.val_j, P.count, P.offset, P.cursor, P.slots, P.scan_tmp};
+                    P.val_j, P.count, P.offset, P.slots, P.scan_tmp};
     for (void *p : ptrs) if (p) cudaFree(p);
     P = Particles{};
 }
@@ -331,20 +418,22 @@ void launch_cpic_phases(Ctx &c, int reassign) {
         return;
     }
     const int gp = grid_for(P.n, B);
-    if (c.nc == 3) k_cpic_push<3><<<gp, B, 0, c.stream>>>(P, (const double *)c.Unext, c.L, reassign);
-    else k_cpic_push<2><<<gp, B, 0, c.stream>>>(P, (const double *)c.Unext, c.L, reassign);
-    cudaMemsetAsync(P.count, 0, sizeof(int) * 4 * V, c.stream);
-    cudaMemsetAsync(P.cursor, 0, sizeof(int) * 4 * V, c.stream);
-    k_cpic_count<<<gp, B, 0, c.stream>>>(P, V);
+    CpicConst K;
+    for (int i = 0; i < 3; i++) {
+        K.inv_a[i] = 1.0 / c.L.a[i];
+        K.a_dt[i] = c.L.a[i] / c.L.dt;
+    }
+    if (c.nc == 3) k_cpic_push<3><<<gp, B, 0, c.stream>>>(P, (const double *)c.Unext, c.L, K, reassign);
+    else k_cpic_push<2><<<gp, B, 0, c.stream>>>(P, (const double *)c.Unext, c.L, K, reassign);
     const long n4 = 4 * V;
-    const long nb = (n4 + SCAN_B - 1) / SCAN_B;
-    k_scan_block<<<(int)nb, SCAN_B, 0, c.stream>>>(P.count, P.offset, P.scan_tmp, n4);
+    const long nb = (n4 + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_block<<<(int)nb, SCAN_B, 0, c.stream>>>(P.count, P.offset, P.scan_tmp, n4 + 1);
     k_scan_sums<<<1, SCAN_B, 0, c.stream>>>(P.scan_tmp, nb);
-    k_scan_add<<<(int)nb, SCAN_B, 0, c.stream>>>(P.offset, P.scan_tmp, n4);
+    k_scan_add<<<(int)nb, SCAN_B, 0, c.stream>>>(P.offset, P.scan_tmp, n4 + 1);
     k_cpic_scatter<<<gp, B, 0, c.stream>>>(P, V);
     if (c.nc == 3) k_cpic_segsum<3><<<grid_for(n4, B), B, 0, c.stream>>>(P, V, (double *)c.rho, (double *)c.J);
     else k_cpic_segsum<2><<<grid_for(n4, B), B, 0, c.stream>>>(P, V, (double *)c.rho, (double *)c.J);
-    c.launches += 7;
+    c.launches += 6;
     c.j_nonzero = true;
 }
 

@@ -203,6 +203,68 @@ int ic_init_random(Ctx &c, uint64_t seed, double sigma_a, double sigma_e) {
     return OPX_OK;
 }
 
+// div and divT on FP64 fields with the FP64 links U64 (NA components per site)
+void ic_div(Ctx &c, const double *U64, const double *El, double *o) {
+    if (c.nc == 2) k_div<2><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>(U64, El, c.L, o);
+    else k_div<3><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>(U64, El, c.L, o);
+    c.launches++;
+}
+void ic_divT(Ctx &c, const double *U64, const double *l, double *o, int acc) {
+    if (c.nc == 2) k_divT<2><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>(U64, l, c.L, o, acc);
+    else k_divT<3><<<grid_for(c.L.V, 128), 128, 0, c.stream>>>(U64, l, c.L, o, acc);
+    c.launches++;
+}
+
+// x = K^+ b for the covariant Laplacian K = div divT of the links U64, by
+// conjugate gradients from x = 0 until |r| <= tol_rel |b| (b in the range of
+// div, so the iterates stay orthogonal to K's null space).
+int ic_covariant_solve(Ctx &c, const double *U64, const double *b, double *x, double tol_rel, int maxit,
+                       int *iters) {
+    const long ns = c.L.V * c.na, nl = ns * 3;
+    const int B = 256;
+    std::vector<double *> bufs;
+    auto alloc = [&](size_t n) -> double * {
+        double *p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) return nullptr;
+        bufs.push_back(p);
+        return p;
+    };
+    double *r = alloc(ns), *p = alloc(ns), *Ap = alloc(ns), *tl = alloc(nl);
+    if (!r || !p || !Ap || !tl) {
+        for (double *q : bufs) cudaFree(q);
+        cudaGetLastError();
+        c.err = "covariant Laplacian solve: out of device memory";
+        return OPX_ERR_NOMEM;
+    }
+    Dot dot(c);
+    cudaMemsetAsync(x, 0, ns * sizeof(double), c.stream);
+    cudaMemcpyAsync(r, b, ns * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemcpyAsync(p, b, ns * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    double rr = dot(r, r, ns);
+    const double stop = tol_rel * tol_rel * rr;
+    int it = 0;
+    while (it < maxit && rr > stop && rr > 0) {
+        ic_divT(c, U64, p, tl, 0);
+        ic_div(c, U64, tl, Ap);
+        const double pAp = dot(p, Ap, ns);
+        if (!(pAp > 0)) break;
+        const double alpha = rr / pAp;
+        k_axpy<<<grid_for(ns, B), B, 0, c.stream>>>(x, p, alpha, ns);
+        k_axpy<<<grid_for(ns, B), B, 0, c.stream>>>(r, Ap, -alpha, ns);
+        const double rr2 = dot(r, r, ns);
+        k_xpby<<<grid_for(ns, B), B, 0, c.stream>>>(p, r, rr2 / rr, ns);
+        c.launches += 3;
+        rr = rr2;
+        it++;
+    }
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    for (double *q : bufs) cudaFree(q);
+    if (iters) *iters = it;
+    if (e != cudaSuccess) { c.err = std::string("covariant Laplacian solve: ") + cudaGetErrorString(e); return OPX_ERR_CUDA; }
+    if (rr > stop && rr > 0) { c.err = "covariant Laplacian solve: no convergence"; return OPX_ERR_NUMERIC; }
+    return OPX_OK;
+}
+
 int ic_gauss_project(Ctx &c, double tol, int maxit, int *iters, double *final_g2) {
     const long V = c.L.V;
     const int NA = c.na;

@@ -27,7 +27,7 @@ struct Particles {
     // deposition scratch
     int *key_rho = nullptr, *key_j = nullptr;                   // [n]
     double *val_rho = nullptr, *val_j = nullptr;                // [na_ref][n]
-    int *count = nullptr, *offset = nullptr, *cursor = nullptr; // [4V] (+1)
+    int *count = nullptr, *offset = nullptr;                    // [4V + 1]: bucket sizes (zero between steps), their scan
     int *slots = nullptr;                                       // [2n]
     int *scan_tmp = nullptr;
     long scan_tmp_len = 0;
@@ -166,6 +166,12 @@ void launch_alg_to_host(Ctx &c, const void *src, double *dst, int ndir, int layo
 // ---- initial conditions (ic_kernels.cu) ----
 int ic_init_random(Ctx &c, uint64_t seed, double sigma_a, double sigma_e);
 int ic_gauss_project(Ctx &c, double tol, int maxit, int *iters, double *final_g2);
+// FP64 covariant divergence of a link-algebra field and its transpose (ic_kernels.cu):
+//   (div E)(x) = sum_i c_i [E_i(x) - Ad(U_i(x-i)^dag) E_i(x-i)],  (divT l)_i(x) = c_i [l(x) - Ad(U_i(x)) l(x+i)]
+void ic_div(Ctx &c, const double *U64, const double *El, double *o);
+void ic_divT(Ctx &c, const double *U64, const double *l, double *o, int acc);
+// x = K^+ b, K = div divT, by conjugate gradients (|r| <= tol_rel |b|)
+int ic_covariant_solve(Ctx &c, const double *U64, const double *b, double *x, double tol_rel, int maxit, int *iters);
 // ---- CPIC (cpic_kernels.cu) ----
 int cpic_alloc(Ctx &c, long n);
 void cpic_free(Ctx &c);

@@ -8,29 +8,43 @@ write the reference's file formats.
   ProjectedEnergyDensity diagnostics/methods/ProjectedEnergyDensity.java (TSV rows, :91-105, :114-179)
 """
 import decimal
+import math
 import os
 import struct
 import time
 
 import numpy as np
 
-_D = decimal.Context(prec=17, rounding=decimal.ROUND_HALF_EVEN)
+def java_round(x):
+    """Math.round(double): the nearest integer, halves rounded up (the Java 7+
+    definition, in which 0.49999999999999994 rounds to 0)."""
+    x = float(x)
+    r = math.floor(x)
+    return int(r) + (1 if x - r >= 0.5 else 0)
 
 
 def java_sci(x):
     """java.text.DecimalFormat("0.################E0").format(x): one integer
-    digit, up to 16 fraction digits (HALF_EVEN), no '+' in the exponent."""
+    digit, up to 16 fraction digits, no '+' in the exponent.  DecimalFormat
+    starts from the digits of Double.toString (DigitList.set(double) takes
+    FloatingDecimal's shortest round-trip digits) and rounds them (HALF_EVEN)
+    only beyond the pattern's 17 significant digits, which the shortest digits
+    of a double never exceed: the mantissa is the shortest round-trip digits
+    (the digits of JDK 19+ Double.toString; older JDKs print one digit more
+    for a few rare values)."""
     x = float(x)
     if x != x:
         return "NaN"
     if x in (float("inf"), float("-inf")):
-        return ("-" if x < 0 else "") + "∞"
+        return ("-" if x < 0 else "") + "\u221e"
     if x == 0.0:
-        return ("-" if str(x).startswith("-") else "") + "0E0"
-    d = _D.create_decimal(x)
-    sign, digits, exp = d.as_tuple()
-    ds = "".join(str(v) for v in digits).rstrip("0") or "0"
-    e10 = exp + len(digits) - 1
+        return ("-" if math.copysign(1.0, x) < 0 else "") + "0E0"
+    sign, digits, exp = decimal.Decimal(repr(x)).as_tuple()
+    ds = "".join(str(v) for v in digits)
+    lead = len(ds) - len(ds.lstrip("0"))
+    ds = ds.lstrip("0")
+    e10 = exp + len(digits) - lead - 1
+    ds = ds.rstrip("0") or "0"
     mant = ds[0] + ("." + ds[1:] if len(ds) > 1 else "")
     return ("-" if sign else "") + mant + "E" + str(e10)
 
@@ -84,7 +98,7 @@ class BulkQuantitiesInTime(Diagnostics):
 
     def initialize(self, s):
         self.s = s
-        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        self.stepInterval = max(java_round(self.timeInterval / s.getTimeStep()), 1)
         if not self.supressOutput:
             with open(self.path, "w") as f:
                 f.write(self.HEADER + "\n")
@@ -117,17 +131,24 @@ class EnergyDensity(Diagnostics):
         self.counter = 0
         self.last = None
 
+    def file_for(self, counter):
+        """FilenameUtils.concat(getPath(f), getBaseName(f) + "_" + counter + "." + getExtension(f))
+        (EnergyDensity.java:62-67): the dot stays when the name has no extension."""
+        head, name = os.path.split(self.filename)
+        dot = name.rfind(".")
+        base, ext = (name[:dot], name[dot + 1:]) if dot >= 0 else (name, "")
+        return os.path.join(head, f"{base}_{counter}.{ext}")
+
     def initialize(self, s):
-        self.firstStep = int(max(round(self.startTime / s.getTimeStep()), 1))
-        self.step = int(round(self.timeInterval / s.getTimeStep()))
+        self.firstStep = max(java_round(self.startTime / s.getTimeStep()), 1)
+        self.step = java_round(self.timeInterval / s.getTimeStep())
         self.s = s
 
     def calculate(self, grid, particles, steps):
         if steps % self.step != 0 or steps < self.firstStep:
             return
         self.counter += 1
-        base, ext = os.path.splitext(self.filename)
-        path = f"{base}_{self.counter}{ext}"
+        path = self.file_for(self.counter)
         e = grid.energy_density()
         self.last = e
         with open(path, "wb") as f:
@@ -148,7 +169,7 @@ class ProjectedEnergyDensity(Diagnostics):
         self.last_poynting = None
 
     def initialize(self, s):
-        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        self.stepInterval = max(java_round(self.timeInterval / s.getTimeStep()), 1)
         open(self.path, "w").close()
 
     def calculate(self, grid, particles, steps):
@@ -205,7 +226,7 @@ class OccupationNumbersInTime(Diagnostics):
             open(path, "w").close()
 
     def initialize(self, s):
-        self.stepInterval = int(max(round(self.timeInterval / s.getTimeStep()), 1))
+        self.stepInterval = max(java_round(self.timeInterval / s.getTimeStep()), 1)
         dims = s.grid.dims
         if self.outputType == "none":
             return
@@ -254,7 +275,7 @@ class TimeMeasurement(Diagnostics):
         self.interval = float(interval)
 
     def initialize(self, s):
-        self.stepInterval = int(max(round(self.interval / s.getTimeStep()), 1))
+        self.stepInterval = max(java_round(self.interval / s.getTimeStep()), 1)
         self.t0 = time.perf_counter()
         open(self.path, "w").close()
 

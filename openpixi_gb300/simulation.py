@@ -323,10 +323,10 @@ class Simulation:
             self.step()
 
     def _measured_loop(self):
-        from .diagnostics import BulkQuantitiesInTime
+        from .diagnostics import BulkQuantitiesInTime, java_round
         if not self.diagnostics or not all(type(d) is BulkQuantitiesInTime for d in self.diagnostics):
             return False
-        return all(max(round(d.timeInterval / self.tstep), 1) == 1 for d in self.diagnostics)
+        return all(max(java_round(d.timeInterval / self.tstep), 1) == 1 for d in self.diagnostics)
 
     def runDiagnostics(self):
         for d in self.diagnostics:
