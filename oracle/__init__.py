@@ -196,6 +196,10 @@ class OracleGrid:
     def update_grid(self):
         lib().orc_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext), _p(self.active))
 
+    def update_grid_tym(self):
+        """TemporalYangMillsSolver.step (the plaquette form) in place of update_grid."""
+        lib().orc_update_grid_tym(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext), _p(self.active))
+
     def update_grid_implicit(self, iterations, damping):
         """ImplicitTYMSolver.step (SU(2), SU(3)) in place of update_grid."""
         rc = lib().orc_implicit_update_grid(self.pp, _p(self.U), _p(self.E), _p(self.J), _p(self.Unext),

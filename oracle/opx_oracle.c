@@ -824,6 +824,46 @@ void orc_update_links(const orc_params *p, const double *U, const double *E, dou
     }
 }
 
+/* TemporalYangMillsSolver.step (physics/fields/TemporalYangMillsSolver.java:24-40):
+ * the same equations as FastTYMSolver in plaquette form, in two passes over
+ * the cells.  UpdateFields.execute (:58-73): for each direction i,
+ * temp = sum_{j != i} [getPlaquette(x, i, j, 1, 1, 0) + getPlaquette(x, i, j, 1, -1, 0)]
+ * * (dt / a_j^2), then E_i += proj(temp) and E_i += J_i * (-dt * g a_i);
+ * UpdateLinks.execute (:83-93) as FastTYMSolver's. */
+void orc_update_grid_tym(const orc_params *p, const double *U, double *E, const double *J,
+                         double *Unext, const uint8_t *active)
+{
+    int nc = p->nc, ng = orc_ng(nc), na = orc_na(nc);
+    long Vn = vol(p);
+    double plaquetteFactor[3], unitFactor[3];
+    for (int j = 0; j < 3; j++) {
+        plaquetteFactor[j] = p->dt / pow(p->a[j], 2);
+        unitFactor[j] = -p->dt * (p->g * p->a[j]);
+    }
+    for (long x = 0; x < Vn; x++) {
+        if (active && !active[x]) continue;
+        for (int i = 0; i < 3; i++) {
+            double temp[NG_MAX], P[NG_MAX], pr[NA_MAX];
+            memset(temp, 0, sizeof(double) * ng);
+            for (int j = 0; j < 3; j++) {
+                if (j == i) continue;
+                orc_plaquette(p, U, x, i, j, 1, 1, P);
+                for (int k = 0; k < ng; k++) P[k] = P[k] * plaquetteFactor[j];
+                for (int k = 0; k < ng; k++) temp[k] = temp[k] + P[k];
+                orc_plaquette(p, U, x, i, j, 1, -1, P);
+                for (int k = 0; k < ng; k++) P[k] = P[k] * plaquetteFactor[j];
+                for (int k = 0; k < ng; k++) temp[k] = temp[k] + P[k];
+            }
+            double *Ei = E + ((size_t)x * 3 + i) * na;
+            const double *Ji = J + ((size_t)x * 3 + i) * na;
+            orc_group_proj(nc, temp, pr);
+            for (int c = 0; c < na; c++) Ei[c] = Ei[c] + pr[c];
+            for (int c = 0; c < na; c++) Ei[c] = Ei[c] + Ji[c] * unitFactor[i];
+        }
+    }
+    orc_update_links(p, U, E, Unext, active);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Reductions                                                                 */
 /* ------------------------------------------------------------------------- */

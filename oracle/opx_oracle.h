@@ -77,6 +77,9 @@ void orc_gauss_constraint(const orc_params *p, const double *U, const double *E,
 /* ---- leapfrog (physics/fields/FastTYMSolver.java) ---- */
 void orc_update_grid(const orc_params *p, const double *U, double *E, const double *J,
                      double *Unext, const uint8_t *active);
+/* TemporalYangMillsSolver.step: the plaquette form, E pass then link pass */
+void orc_update_grid_tym(const orc_params *p, const double *U, double *E, const double *J,
+                         double *Unext, const uint8_t *active);
 void orc_update_links(const orc_params *p, const double *U, const double *E,
                       double *Unext, const uint8_t *active);
 /* Same algorithm split over host threads (OpenMP); timed CPU baseline only. */
