@@ -362,9 +362,12 @@ int opx_objective_gradient(opx_ctx *ctx, const opx_objective *obj, int nsteps, i
 
 /* ---- batching form: many independent lattices ("events") in one launch ----
  * The reference runs one Simulation per event (a loop over independent
- * Simulation objects); here every event advances in one persistent launch of
- * thread-block clusters, each cluster owning a load-balanced set of events,
- * captured in a CUDA graph.  Events are pure Yang-Mills (no particles).
+ * Simulation objects); here the events advance together under one of two
+ * schedules, both captured in a CUDA graph: one persistent launch of
+ * thread-block clusters, each cluster owning a load-balanced set of events for
+ * every step (cluster size 1-8), or the flat schedule (cluster size 0), one
+ * launch per step over the sites of all events.  Events are pure Yang-Mills
+ * (no particles).
  * dims: [nevents][3]; a: [nevents][3] lattice spacings or NULL (all 1). */
 typedef struct opx_batch opx_batch;
 int opx_batch_create(int ncolors, int nevents, const int *dims, const double *a, double dt, double g,
@@ -378,11 +381,16 @@ int opx_batch_upload(opx_batch *b, int event, int field, const double *host, siz
 int opx_batch_download(opx_batch *b, int event, int field, double *host, size_t count, int layout);
 /* Simulation.initialize (stepLinks) for every event */
 int opx_batch_initialize(opx_batch *b);
-/* Pick the cluster size and block size by timing `steps` steps of each
- * candidate on the batch itself (the fields are restored afterwards). */
+/* Pick the schedule (cluster size 0 = flat, or 1, 2, 4, 8) and block size by
+ * timing `steps` steps of each candidate on the batch itself (the fields are
+ * restored afterwards). */
 int opx_batch_autotune(opx_batch *b, int steps, int *cluster, int *block);
-/* nsteps x Simulation.step (no diagnostics) of every event in one launch;
- * use_graph != 0 replays a captured CUDA graph of that launch. */
+/* Set the schedule directly: cluster 0 (flat) or 1, 2, 4, 8 with block 128 or
+ * 256; OPX_ERR_UNSUPPORTED if that launch does not fit (SU(3) FP32: block 128). */
+int opx_batch_set_schedule(opx_batch *b, int cluster, int block);
+/* nsteps x Simulation.step (no diagnostics) of every event: one launch
+ * (clusters) or nsteps launches (flat); use_graph != 0 replays a captured CUDA
+ * graph of them. */
 int opx_batch_run(opx_batch *b, int nsteps, int use_graph);
 int opx_batch_time_run(opx_batch *b, int nsteps, int use_graph, double *ms);
 /* BulkQuantities of every event (out[nevents]), FP64 compensated sums */

@@ -41,6 +41,7 @@ EXPORTED = [
     "opx_objective_value", "opx_objective_tangent", "opx_objective_gradient",
     "opx_batch_create", "opx_batch_destroy", "opx_batch_last_error", "opx_batch_init_random",
     "opx_batch_upload", "opx_batch_download", "opx_batch_initialize", "opx_batch_autotune",
+    "opx_batch_set_schedule",
     "opx_batch_run", "opx_batch_time_run", "opx_batch_reduce", "opx_batch_config",
     "opx_batch_kernel_launches",
     "opx_energy_objective", "opx_energy_tangent", "opx_energy_gradient", "opx_cgc_mv",
@@ -149,6 +150,7 @@ def load(path=None):
         "opx_batch_download": (C.c_int, [vp, C.c_int, C.c_int, vp, sz, C.c_int]),
         "opx_batch_initialize": (C.c_int, [vp]),
         "opx_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "opx_batch_set_schedule": (C.c_int, [vp, C.c_int, C.c_int]),
         "opx_batch_run": (C.c_int, [vp, C.c_int, C.c_int]),
         "opx_batch_time_run": (C.c_int, [vp, C.c_int, C.c_int, dp]),
         "opx_batch_reduce": (C.c_int, [vp, vp]),
@@ -573,6 +575,10 @@ class Batch:
         c, b = C.c_int(), C.c_int()
         self.check(self.L.opx_batch_autotune(self.h, int(steps), C.byref(c), C.byref(b)))
         return c.value, b.value
+
+    def set_schedule(self, cluster, block):
+        """cluster 0: one launch per step over all events; 1-8: persistent clusters."""
+        self.check(self.L.opx_batch_set_schedule(self.h, int(cluster), int(block)))
 
     def run(self, nsteps, use_graph=True):
         self.check(self.L.opx_batch_run(self.h, int(nsteps), 1 if use_graph else 0))

@@ -250,7 +250,7 @@ int opx_upload(opx_ctx *ctx, int field, const double *host, size_t count, int la
     case OPX_FIELD_UNEXT: launch_links_from_ref(c, src, c.Unext); break;
     case OPX_FIELD_E: launch_alg_from_host(c, src, c.E, 3, layout); break;
     case OPX_FIELD_J: launch_alg_from_host(c, src, c.J, 3, layout); c.j_nonzero = true; break;
-    case OPX_FIELD_RHO: launch_alg_from_host(c, src, c.rho, 1, layout); break;
+    case OPX_FIELD_RHO: launch_alg_from_host(c, src, c.rho, 1, layout); c.rho_nonzero = true; break;
     }
     return sync_check(c, "opx_upload");
 }

@@ -106,6 +106,51 @@ __global__ void __launch_bounds__(128, 3) k_batch_persistent_su3f(const BEvent<f
     }
 }
 
+// Flat schedule: one launch per step over the sites of all events, each block
+// inside one event (blocks of event order[q] start at bstart[q]; events in
+// decreasing size), no cluster.  The hardware block scheduler balances the
+// load, and a step costs one launch (replayed from a CUDA graph) instead of a
+// cluster barrier.  rd: the buffer holding U (Unext is rd ^ 1).
+__device__ __forceinline__ int flat_event(const int *__restrict__ bstart, int nev, int b) {
+    int lo = 0, hi = nev - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(bstart + mid) <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int NC, typename R, typename I, bool REUNIT>
+__global__ void __launch_bounds__(256) k_batch_flat(const BEvent<R> *__restrict__ ev, const int *__restrict__ order,
+                                                    const int *__restrict__ bstart, int nev, int rd) {
+    const int q = flat_event(bstart, nev, (int)blockIdx.x);
+    const BEvent<R> &e = ev[order[q]];
+    const I s = (I)((int)blockIdx.x - bstart[q]) * (I)blockDim.x + (I)threadIdx.x;
+    if (s >= (I)e.L.V) return;
+    update_site<NC, R, false, REUNIT, I>(e.B[rd], e.E, nullptr, e.B[rd ^ 1], e.L, s);
+}
+
+// SU(3) FP32, paired: thread slot t of an event covers sa = 64 (t / 32) + t % 32, sb = sa + 32
+template <typename I, bool REUNIT>
+__global__ void __launch_bounds__(128, 3) k_batch_flat_su3f(const BEvent<float> *__restrict__ ev,
+                                                            const int *__restrict__ order,
+                                                            const int *__restrict__ bstart, int nev, int rd) {
+    const int q = flat_event(bstart, nev, (int)blockIdx.x);
+    const BEvent<float> &e = ev[order[q]];
+    const I t = (I)((int)blockIdx.x - bstart[q]) * (I)blockDim.x + (I)threadIdx.x;
+    const I V = (I)e.L.V, sa = ((t >> 5) << 6) + (t & 31);
+    if (sa >= V) return;
+    I sb = sa + 32;
+    const bool vb = sb < V;
+    if (!vb) sb = sa;
+    update_site_pair<I, false, REUNIT>(e.B[rd], e.E, nullptr, e.B[rd ^ 1], e.L, sa, sb, true, vb);
+}
+
+template <int NC, typename R, typename I, bool REUNIT> static void *flat_kernel() {
+    if constexpr (NC == 3 && sizeof(R) == 4) return (void *)k_batch_flat_su3f<I, REUNIT>;
+    else return (void *)k_batch_flat<NC, R, I, REUNIT>;
+}
+
 // the persistent kernel of a batch's group and precision
 template <int NC, typename R, typename I> static void *persistent_kernel() {
     if constexpr (NC == 3 && sizeof(R) == 4) return (void *)k_batch_persistent_su3f<I>;
@@ -164,8 +209,12 @@ struct Batch {
     long steps = 0;
     cudaStream_t stream = nullptr;
     // schedule
+    // cluster 0: the flat schedule (one launch per step, order_dev / bstart_dev,
+    // flat_blocks blocks); otherwise persistent clusters (list_dev / begin_dev)
     int cluster = 0, block = 0, nclusters = 0;
     int *list_dev = nullptr, *begin_dev = nullptr;
+    int *order_dev = nullptr, *bstart_dev = nullptr;
+    int flat_blocks = 0;
     std::map<std::tuple<int, int, long>, cudaGraphExec_t> graphs;  // (nsteps, cur, step phase) -> graph
     double *red_part = nullptr, *red_out = nullptr, *red_host = nullptr;
     std::string err;
@@ -202,7 +251,7 @@ static void drop_graphs(Batch &b) {
 
 static void batch_release(Batch &b) {
     drop_graphs(b);
-    void *p[] = {b.store, b.ev_dev, b.list_dev, b.begin_dev, b.red_part, b.red_out};
+    void *p[] = {b.store, b.ev_dev, b.list_dev, b.begin_dev, b.order_dev, b.bstart_dev, b.red_part, b.red_out};
     for (void *x : p) if (x) cudaFree(x);
     if (b.red_host) cudaFreeHost(b.red_host);
     if (b.stream) cudaStreamDestroy(b.stream);
@@ -248,8 +297,50 @@ static void schedule(Batch &b, int nclusters) {
     b.nclusters = nclusters;
 }
 
+// Flat schedule: events in decreasing size, each one's thread units (sites, or
+// site pairs for SU(3) FP32) in blocks of b.block.
+static void schedule_flat(Batch &b, int block) {
+    std::vector<int> order(b.nev);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b.lats[x].V > b.lats[y].V; });
+    const bool paired = b.nc == 3 && b.prec == OPX_F32;
+    std::vector<int> bstart(1, 0);
+    for (int q : order) {
+        const long V = b.lats[q].V, units = paired ? ((V + 63) >> 6) << 5 : V;
+        bstart.push_back(bstart.back() + (int)((units + block - 1) / block));
+    }
+    if (b.order_dev) cudaFree(b.order_dev);
+    if (b.bstart_dev) cudaFree(b.bstart_dev);
+    cudaMalloc(&b.order_dev, sizeof(int) * order.size());
+    cudaMalloc(&b.bstart_dev, sizeof(int) * bstart.size());
+    cudaMemcpy(b.order_dev, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(b.bstart_dev, bstart.data(), sizeof(int) * bstart.size(), cudaMemcpyHostToDevice);
+    b.flat_blocks = bstart.back();
+    b.nclusters = 0;
+}
+
+template <int NC, typename R>
+static cudaError_t launch_flat(Batch &b, int nsteps, cudaStream_t st) {
+    const long step0 = b.reunit_every > 0 ? b.steps % b.reunit_every : 0L;
+    const BEvent<R> *ev = (const BEvent<R> *)b.ev_dev;
+    const int *order = b.order_dev, *bstart = b.bstart_dev;
+    int nev = b.nev;
+    for (int k = 0; k < nsteps; k++) {
+        const bool reunit = b.reunit_every > 0 && ((step0 + k + 1) % b.reunit_every) == 0;
+        int rd = b.cur ^ ((k + 1) & 1);
+        void *args[] = {(void *)&ev, (void *)&order, (void *)&bstart, (void *)&nev, (void *)&rd};
+        void *kf = b.int_offsets ? (reunit ? flat_kernel<NC, R, int, true>() : flat_kernel<NC, R, int, false>())
+                                 : (reunit ? flat_kernel<NC, R, long, true>() : flat_kernel<NC, R, long, false>());
+        cudaError_t e = cudaLaunchKernel(kf, dim3(b.flat_blocks), dim3(b.block), args, 0, st);
+        b.launches++;
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 template <int NC, typename R>
 static cudaError_t launch_persistent(Batch &b, int nsteps, cudaStream_t st) {
+    if (b.cluster == 0) return launch_flat<NC, R>(b, nsteps, st);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(b.nclusters * b.cluster);
     cfg.blockDim = dim3(b.block);
@@ -305,6 +396,14 @@ static int occupancy_dispatch(Batch &b, int cluster, int block) {
 }
 
 static int configure(Batch &b, int cluster, int block) {
+    if (cluster == 0) {
+        if (b.nc == 3 && b.prec == OPX_F32 && block > 128) return OPX_ERR_UNSUPPORTED;  // the paired kernel's bound
+        b.cluster = 0;
+        b.block = block;
+        schedule_flat(b, block);
+        drop_graphs(b);
+        return OPX_OK;
+    }
     int n = occupancy_dispatch(b, cluster, block);
     if (n <= 0) return OPX_ERR_UNSUPPORTED;
     b.cluster = cluster;
@@ -508,7 +607,7 @@ static int batch_run(Batch &b, int nsteps, int use_graph) {
             it = b.graphs.emplace(key, ge).first;
         }
         e = cudaGraphLaunch(it->second, b.stream);
-        b.launches++;  // the graph holds one kernel node
+        b.launches += b.cluster == 0 ? nsteps : 1;  // the graph's kernel nodes
     } else {
         e = run_dispatch(b, nsteps, b.stream);
     }
@@ -551,7 +650,7 @@ int opx_batch_autotune(opx_batch *h, int steps, int *cluster_out, int *block_out
     cudaMemcpyAsync(snap, b.store, b.store_bytes, cudaMemcpyDeviceToDevice, b.stream);
     const int cur0 = b.cur;
     const long steps0 = b.steps;
-    const int clusters[] = {1, 2, 4, 8};
+    const int clusters[] = {0, 1, 2, 4, 8};  // 0: the flat schedule
     const int blocks[] = {128, 256};
     double best = 1e300;
     int bc = b.cluster, bb = b.block;
@@ -584,6 +683,19 @@ int opx_batch_autotune(opx_batch *h, int steps, int *cluster_out, int *block_out
     if (block_out) *block_out = b.block;
     if (rc) return batch_fail(b, "opx_batch_autotune: no launch configuration fits", rc);
     return batch_sync(b, "opx_batch_autotune");
+}
+
+int opx_batch_set_schedule(opx_batch *h, int cluster, int block) {
+    if (!h || (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) ||
+        (block != 128 && block != 256))
+        return OPX_ERR_INVALID;
+    Batch &b = h->b;
+    const int c0 = b.cluster, b0 = b.block;
+    if (configure(b, cluster, block) != OPX_OK) {
+        configure(b, c0, b0);
+        return batch_fail(b, "opx_batch_set_schedule: that launch configuration does not fit", OPX_ERR_UNSUPPORTED);
+    }
+    return batch_sync(b, "opx_batch_set_schedule");
 }
 
 int opx_batch_reduce(opx_batch *h, opx_observables *out) {

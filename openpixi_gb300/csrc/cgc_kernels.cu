@@ -120,6 +120,11 @@ __global__ void k_wilson_scan(const double *__restrict__ phi, double *__restrict
     if (t >= ntr) return;
     const long V = (long)n0 * ntr;
     const LinkPlanes<G, double> Vp{Vl, V};  // direction slot 0 holds V
+    // each sheet's V is the previous sheet's (kept in registers: the loads of
+    // LinkPlanes go through the read-only cache, which must not see this
+    // kernel's own stores) times one exponential; the first reads the identity
+    const int z0 = orientation < 0 ? 0 : n0 - 1;
+    auto prev = Vp.load(0, (long)(((z0 + orientation) % n0 + n0) % n0) * ntr + t);
     for (int k = 0; k < n0; k++) {
         const int z = orientation < 0 ? k : (n0 - k - 1);
         const long idx = (long)z * ntr + t;
@@ -128,7 +133,8 @@ __global__ void k_wilson_scan(const double *__restrict__ phi, double *__restrict
         const long src = orientation == -1 ? idxL : idx;
         double x[NA];
         for (int a = 0; a < NA; a++) x[a] = phi[(long)a * V + src] * gaugeFactor;
-        Vp.store(0, idx, G::mul(Vp.load(0, idxL), G::expi(x)));
+        prev = G::mul(prev, G::expi(x));
+        Vp.store(0, idx, prev);
     }
 }
 

@@ -410,6 +410,7 @@ void cpic_free(Ctx &c) {
 
 void launch_cpic_phases(Ctx &c, int reassign) {
     Particles &P = c.P;
+    c.rho_nonzero = true;
     const long V = c.L.V;
     const int B = 256;
     if (P.n == 0) {
@@ -568,6 +569,7 @@ static bool super_needs_update(int orientation, int shift, int ppc, long t) {
 }
 
 void launch_super_phases(Ctx &c, long t) {
+    c.rho_nonzero = true;
     const long V = c.L.V, ntr = V / c.L.n[0];
     const int ppc = c.sg_ppc, nar = c.na_ref;
     SuperStep cin{}, jin{};

@@ -141,7 +141,8 @@ int measured_blocks(const Ctx &c) { return grid_for(((c.L.V + 63) / 64) * 32, ME
 // into c.E and Wout into Win).
 void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, void *Wout, double *part) {
     const int nb = measured_blocks(c);
-    const float *U = (const float *)c.U, *rho = (const float *)c.rho, *Wi = (const float *)Win;
+    const float *U = (const float *)c.U, *rho = c.rho_nonzero ? (const float *)c.rho : nullptr;
+    const float *Wi = (const float *)Win;
     float *E = (float *)c.E, *Eo = (float *)Eout, *Un = (float *)c.Unext, *Wo = (float *)Wout;
     if (c.int_offsets) {
         if (reunit) k_update_measure_su3f_pair<int, true><<<nb, MEAS_THREADS, 0, c.stream>>>(U, E, Eo, Wi, Wo, rho, Un, c.L, part);

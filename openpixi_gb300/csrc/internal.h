@@ -52,6 +52,9 @@ struct Ctx {
     void *U = nullptr, *Unext = nullptr, *E = nullptr, *J = nullptr, *rho = nullptr;
     uint8_t *active = nullptr, *eval = nullptr;  // null = all true
     bool j_nonzero = false;
+    // rho has been written (an upload or the particle phases); until then it is
+    // zero and the kernels that subtract it from the Gauss law skip its loads
+    bool rho_nonzero = false;
     // SU(3) FP32 leapfrog and reduction with two sites per thread in paired FP32
     // instructions (environment OPX_ONE_SITE_FP32=1 selects the
     // one-site-per-thread forms)

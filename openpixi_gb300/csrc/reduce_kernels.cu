@@ -308,20 +308,20 @@ static void bulk_t(Ctx &c, int skip_u) {
             static const int wave = resident_blocks(k_bulk_partial_su3f_pair<int>);
             nb = std::min(nb, wave);
             k_bulk_partial_su3f_pair<int><<<nb, RED_THREADS, 0, c.stream>>>(
-                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
+                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)(c.rho_nonzero ? c.rho : nullptr), c.eval, c.L,
                 skip_u, c.red_part, c.red_count, c.red_out);
         } else {
             static const int wave = resident_blocks(k_bulk_partial_su3f_pair<long>);
             nb = std::min(nb, wave);
             k_bulk_partial_su3f_pair<long><<<nb, RED_THREADS, 0, c.stream>>>(
-                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)c.rho, c.eval, c.L,
+                (const float *)c.U, (const float *)c.Unext, (const float *)c.E, (const float *)(c.rho_nonzero ? c.rho : nullptr), c.eval, c.L,
                 skip_u, c.red_part, c.red_count, c.red_out);
         }
     } else {
         static const int wave = resident_blocks(k_bulk_partial<NC, R>);
         nb = std::min(nb, wave);
         k_bulk_partial<NC, R><<<nb, RED_THREADS, 0, c.stream>>>((const R *)c.U, (const R *)c.Unext, (const R *)c.E,
-                                                               (const R *)c.rho, c.eval, c.L, skip_u, c.red_part,
+                                                               (const R *)(c.rho_nonzero ? c.rho : nullptr), c.eval, c.L, skip_u, c.red_part,
                                                                c.red_count, c.red_out, c.bn_site);
     }
     c.launches += 1;

@@ -660,8 +660,10 @@ __device__ __forceinline__ pr::P gauss_w_pair(const float *__restrict__ E, const
             gs[a] = fma2(sub2(e0, w), gf, gs[a]);
         }
     }
+    if (rho) {
 #pragma unroll
-    for (int a = 0; a < 8; a++) gs[a] = sub2(gs[a], pp(__ldg(rho + (I)a * V + sa), __ldg(rho + (I)a * V + sb)));
+        for (int a = 0; a < 8; a++) gs[a] = sub2(gs[a], pp(__ldg(rho + (I)a * V + sa), __ldg(rho + (I)a * V + sb)));
+    }
     P g2 = mul2(gs[0], gs[0]);
 #pragma unroll
     for (int a = 1; a < 8; a++) g2 = fma2(gs[a], gs[a], g2);
