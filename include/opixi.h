@@ -410,7 +410,8 @@ long opx_batch_kernel_launches(const opx_batch *b);
  * blocks [3][ceil(V/32)][18][32], SU(2) links as [3][32 ceil(V/32)][4]
  * (quaternion components contiguous), algebra fields as planes E [3][ngen][V],
  * rho [ngen][V] (NULL = zero charge), eval [V] (NULL = all cells), elements
- * double (OPX_F64) or float (OPX_F32).
+ * double (OPX_F64) or float (OPX_F32).  U and Unext must be 16-byte aligned
+ * (OPX_ERR_INVALID otherwise; cudaMalloc'd buffers are).
  * Calls no cudaMalloc/cudaFree: its scratch is a fixed 77,824-byte __device__
  * array of the library, held by every GPU that loads the library until exit.
  * Limit: V <= 2^29 sites (larger lattices return OPX_ERR_INVALID).  The first

@@ -120,6 +120,9 @@ extern "C" int opx_reduce_noalloc(int ncolors, int precision, const int *dims, c
     if ((ncolors != 2 && ncolors != 3) || (precision != OPX_F64 && precision != OPX_F32) || !dims || !a ||
         !U || !Unext || !E || !out_device || !(g > 0))
         return OPX_ERR_INVALID;
+    // SU(2) links are read as 16-byte vectors: a misaligned buffer is refused here
+    // rather than faulting on the device
+    if (((uintptr_t)U | (uintptr_t)Unext) & 15) return OPX_ERR_INVALID;
     long V = 1;
     for (int i = 0; i < 3; i++) {
         if (dims[i] < 1 || !(a[i] > 0)) return OPX_ERR_INVALID;

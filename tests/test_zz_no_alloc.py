@@ -122,3 +122,8 @@ def test_noalloc_rejects_oversize(native):
     a_c = (C.c_double * 3)(1.0, 1.0, 1.0)
     rc = native.opx_reduce_noalloc(2, N.OPX_F64, dims_c, a_c, 1.0, p, p, p, None, None, p, None)
     assert rc == N.OPX_ERR_INVALID
+    # a link buffer that is not 16-byte aligned is refused before any launch
+    dims_s = (C.c_int * 3)(2, 2, 2)
+    q = C.c_void_p(buf.data_ptr() + 8)
+    rc = native.opx_reduce_noalloc(2, N.OPX_F64, dims_s, a_c, 1.0, q, p, p, None, None, p, None)
+    assert rc == N.OPX_ERR_INVALID
