@@ -120,8 +120,13 @@ __device__ __forceinline__ int flat_event(const int *__restrict__ bstart, int ne
     return lo;
 }
 
+// blocks of 256 threads per SM the generic flat kernel is compiled for (SU(2)
+// FP32: 40 registers, as the single-lattice kernel)
+template <int NC, typename R> struct FlatBounds { static constexpr int minb = 1; };
+template <> struct FlatBounds<2, float> { static constexpr int minb = 6; };
+
 template <int NC, typename R, typename I, bool REUNIT>
-__global__ void __launch_bounds__(256) k_batch_flat(const BEvent<R> *__restrict__ ev, const int *__restrict__ order,
+__global__ void __launch_bounds__(256, FlatBounds<NC, R>::minb) k_batch_flat(const BEvent<R> *__restrict__ ev, const int *__restrict__ order,
                                                     const int *__restrict__ bstart, int nev, int rd) {
     const int q = flat_event(bstart, nev, (int)blockIdx.x);
     const BEvent<R> &e = ev[order[q]];
