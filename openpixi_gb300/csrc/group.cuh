@@ -29,6 +29,8 @@ template <typename R> struct Real;
 template <> struct Real<double> {
     static constexpr double eps = 1.1102230246251565e-16;
     OPX_HD static double sqrt_(double x) { return sqrt(x); }
+    OPX_HD static double abs_(double x) { return fabs(x); }
+    OPX_HD static double max_(double a, double b) { return fmax(a, b); }
     OPX_HD static void sincos_(double x, double *s, double *c) {
 #ifdef __CUDA_ARCH__
         sincos(x, s, c);
@@ -40,6 +42,8 @@ template <> struct Real<double> {
 template <> struct Real<float> {
     static constexpr float eps = 5.9604645e-08f;
     OPX_HD static float sqrt_(float x) { return sqrtf(x); }
+    OPX_HD static float abs_(float x) { return fabsf(x); }
+    OPX_HD static float max_(float a, float b) { return fmaxf(a, b); }
     OPX_HD static void sincos_(float x, float *s, float *c) {
 #ifdef __CUDA_ARCH__
         sincosf(x, s, c);
@@ -331,7 +335,8 @@ template <typename R> struct SU3 {
     }
 
     // Gram-Schmidt on rows 0 and 1; row 2 = conj(row0 x row1)
-    OPX_HD OPX_INLINE static void reunit(M &m) {
+    // Gram-Schmidt on rows 0 and 1; row 2 = conj(row0 x row1)
+    OPX_HD OPX_INLINE static void reunit_gs(M &m) {
         R n0 = R(0);
 #pragma unroll
         for (int k = 0; k < 3; k++) n0 += m.r[k] * m.r[k] + m.i[k] * m.i[k];
@@ -364,6 +369,88 @@ template <typename R> struct SU3 {
             R xi = (m.r[a] * m.i[3 + b] + m.i[a] * m.r[3 + b]) - (m.r[b] * m.i[3 + a] + m.i[b] * m.r[3 + a]);
             m.r[6 + k] = xr;
             m.i[6 + k] = -xi;
+        }
+    }
+    // H = m^dagger m (real diagonal, upper entries); returns the largest |H - 1| entry
+    OPX_HD OPX_INLINE static R gram(const M &m, R *hd, R *hr, R *hi) {
+        R dev = R(0);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            R d = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) d += m.r[3 * k + c] * m.r[3 * k + c] + m.i[3 * k + c] * m.i[3 * k + c];
+            hd[c] = d;
+            dev = Real<R>::max_(dev, Real<R>::abs_(d - R(1)));
+        }
+#pragma unroll
+        for (int o = 0; o < 3; o++) {
+            const int r = o == 2 ? 1 : 0, c = o == 0 ? 1 : 2;
+            R re = R(0), im = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                re += m.r[3 * k + r] * m.r[3 * k + c] + m.i[3 * k + r] * m.i[3 * k + c];
+                im += m.r[3 * k + r] * m.i[3 * k + c] - m.i[3 * k + r] * m.r[3 * k + c];
+            }
+            hr[o] = re;
+            hi[o] = im;
+            dev = Real<R>::max_(dev, Real<R>::max_(Real<R>::abs_(re), Real<R>::abs_(im)));
+        }
+        return dev;
+    }
+    // m <- m (3 - H) / 2, one Newton-Schulz step toward the polar factor
+    OPX_HD OPX_INLINE static void newton_schulz(M &m, const R *hd, const R *hr, const R *hi) {
+        M n;
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const R kd = R(1.5) - R(0.5) * hd[c];
+                R re = m.r[3 * r + c] * kd, im = m.i[3 * r + c] * kd;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    if (k == c) continue;
+                    const int o = (k == 0 || c == 0) ? (k + c - 1) : 2;
+                    const R a = R(-0.5) * hr[o], b = R(-0.5) * (k < c ? hi[o] : -hi[o]);
+                    re += m.r[3 * r + k] * a - m.i[3 * r + k] * b;
+                    im += m.r[3 * r + k] * b + m.i[3 * r + k] * a;
+                }
+                n.r[3 * r + c] = re;
+                n.i[3 * r + c] = im;
+            }
+        m = n;
+    }
+    // The nearest unitary matrix (polar factor: Newton-Schulz steps from a
+    // near-unitary m), then the determinant's phase spread evenly over the
+    // rows; Gram-Schmidt first when m is far from unitary (an entry of
+    // m^dagger m off by more than 0.25).  The polar factor removes the
+    // deviation from unitarity without rotating the link, so periodic
+    // reunitarisation of the FP32 form adds no systematic energy drift.
+    OPX_HD OPX_INLINE static void reunit(M &m) {
+        R hd[3], hr[3], hi[3];
+        R dev = gram(m, hd, hr, hi);
+        if (dev > R(0.25)) {
+            reunit_gs(m);
+            dev = gram(m, hd, hr, hi);
+        }
+        newton_schulz(m, hd, hr, hi);
+        // further steps while the last one left more than rounding
+        for (int it = 0; it < 4 && dev > R(1e-3); it++) {
+            dev = gram(m, hd, hr, hi);
+            newton_schulz(m, hd, hr, hi);
+        }
+        // Im det m from the cofactors of row 0
+        const R c0r = (m.r[4] * m.r[8] - m.i[4] * m.i[8]) - (m.r[5] * m.r[7] - m.i[5] * m.i[7]);
+        const R c0i = (m.r[4] * m.i[8] + m.i[4] * m.r[8]) - (m.r[5] * m.i[7] + m.i[5] * m.r[7]);
+        const R c1r = (m.r[5] * m.r[6] - m.i[5] * m.i[6]) - (m.r[3] * m.r[8] - m.i[3] * m.i[8]);
+        const R c1i = (m.r[5] * m.i[6] + m.i[5] * m.r[6]) - (m.r[3] * m.i[8] + m.i[3] * m.r[8]);
+        const R c2r = (m.r[3] * m.r[7] - m.i[3] * m.i[7]) - (m.r[4] * m.r[6] - m.i[4] * m.i[6]);
+        const R c2i = (m.r[3] * m.i[7] + m.i[3] * m.r[7]) - (m.r[4] * m.i[6] + m.i[4] * m.r[6]);
+        const R t = (m.r[0] * c0i + m.i[0] * c0r + m.r[1] * c1i + m.i[1] * c1r + m.r[2] * c2i + m.i[2] * c2r) / R(3);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const R re = m.r[k] + t * m.i[k];
+            m.i[k] = m.i[k] - t * m.r[k];
+            m.r[k] = re;
         }
     }
 };

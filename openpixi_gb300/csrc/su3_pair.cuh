@@ -295,7 +295,7 @@ __device__ __forceinline__ M expi(const P *x) {
 }
 
 // Gram-Schmidt on rows 0 and 1; row 2 = conj(row0 x row1)
-__device__ __forceinline__ void reunit(M &m) {
+__device__ __forceinline__ void reunit_gs(M &m) {
     P n0 = mul2(m.r[0], m.r[0]);
     n0 = fma2(m.i[0], m.i[0], n0);
 #pragma unroll
@@ -336,6 +336,112 @@ __device__ __forceinline__ void reunit(M &m) {
                           fma2(m.r[b], m.i[3 + a], mul2(m.i[b], m.r[3 + a])));
         m.r[6 + k] = xr;
         m.i[6 + k] = neg2(xi);
+    }
+}
+
+// H = m^dagger m: real diagonal hd, upper entries (0,1), (0,2), (1,2) as hr + i hi;
+// returns the largest |H - 1| entry of the two lanes.
+__device__ __forceinline__ float gram(const M &m, P *hd, P *hr, P *hi) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        P d = mul2(m.r[c], m.r[c]);
+        d = fma2(m.i[c], m.i[c], d);
+#pragma unroll
+        for (int k = 1; k < 3; k++) { d = fma2(m.r[3 * k + c], m.r[3 * k + c], d); d = fma2(m.i[3 * k + c], m.i[3 * k + c], d); }
+        hd[c] = d;
+    }
+#pragma unroll
+    for (int o = 0; o < 3; o++) {
+        const int r = o == 2 ? 1 : 0, c = o == 0 ? 1 : 2;
+        P re = mul2(m.r[r], m.r[c]), ip = mul2(m.r[r], m.i[c]), in = mul2(m.i[r], m.r[c]);
+        re = fma2(m.i[r], m.i[c], re);
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+            re = fma2(m.r[3 * k + r], m.r[3 * k + c], fma2(m.i[3 * k + r], m.i[3 * k + c], re));
+            ip = fma2(m.r[3 * k + r], m.i[3 * k + c], ip);
+            in = fma2(m.i[3 * k + r], m.r[3 * k + c], in);
+        }
+        hr[o] = re;
+        hi[o] = sub2(ip, in);
+    }
+    float dev = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        dev = fmaxf(dev, fmaxf(fabsf(hd[c].x - 1.f), fabsf(hd[c].y - 1.f)));
+        dev = fmaxf(dev, fmaxf(fmaxf(fabsf(hr[c].x), fabsf(hr[c].y)), fmaxf(fabsf(hi[c].x), fabsf(hi[c].y))));
+    }
+    return dev;
+}
+
+// One Newton-Schulz step toward the unitary factor of m's polar decomposition:
+// m <- m (3 - m^dagger m) / 2, given H = m^dagger m.
+__device__ __forceinline__ void newton_schulz(M &m, const P *hd, const P *hr, const P *hi) {
+    const P h3 = bc(1.5f), mh = bc(-0.5f);
+    P kd[3], kr[3], ki[3];  // K = (3 - H) / 2, hermitian
+#pragma unroll
+    for (int c = 0; c < 3; c++) { kd[c] = fma2(mh, hd[c], h3); kr[c] = mul2(mh, hr[c]); ki[c] = mul2(mh, hi[c]); }
+    M n;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            P re = mul2(m.r[3 * r + c], kd[c]), im = mul2(m.i[3 * r + c], kd[c]);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (k == c) continue;
+                // K_kc: stored upper entries, lower ones their conjugates
+                const int o = (k == 0 || c == 0) ? (k + c - 1) : 2;
+                const P a = kr[o], b = k < c ? ki[o] : neg2(ki[o]);
+                re = fma2(m.r[3 * r + k], a, fma2(neg2(m.i[3 * r + k]), b, re));
+                im = fma2(m.r[3 * r + k], b, fma2(m.i[3 * r + k], a, im));
+            }
+            n.r[3 * r + c] = re;
+            n.i[3 * r + c] = im;
+        }
+    m = n;
+}
+
+// Reunitarisation of the FP32 form: the nearest unitary matrix (polar factor by
+// Newton-Schulz steps: the deviations met between reunitarisations are ~1e-6,
+// which one step removes to FP32 rounding; a second step above 1e-3), then the determinant's
+// phase spread evenly over the rows (det = 1 to first order in the phase).
+// Unlike Gram-Schmidt, which rotates the link by an amount of the order of its
+// deviation from unitarity, the polar factor only removes the deviation, so the
+// reunitarisation adds no systematic drift to the energy.  Far from unitary
+// (an entry of m^dagger m off by more than 0.25), Gram-Schmidt comes first.
+__device__ __forceinline__ void reunit(M &m) {
+    P hd[3], hr[3], hi[3];
+    float dev = gram(m, hd, hr, hi);
+    if (dev > 0.25f) {
+        reunit_gs(m);
+        dev = gram(m, hd, hr, hi);
+    }
+    newton_schulz(m, hd, hr, hi);
+    if (dev > 1e-3f) {
+        // a second step where the first leaves more than FP32 rounding
+        gram(m, hd, hr, hi);
+        newton_schulz(m, hd, hr, hi);
+    }
+    // Im det m, from the cofactors of row 0
+    const P c0r = sub2(sub2(mul2(m.r[4], m.r[8]), mul2(m.i[4], m.i[8])), sub2(mul2(m.r[5], m.r[7]), mul2(m.i[5], m.i[7])));
+    const P c0i = sub2(add2(mul2(m.r[4], m.i[8]), mul2(m.i[4], m.r[8])), add2(mul2(m.r[5], m.i[7]), mul2(m.i[5], m.r[7])));
+    const P c1r = sub2(sub2(mul2(m.r[5], m.r[6]), mul2(m.i[5], m.i[6])), sub2(mul2(m.r[3], m.r[8]), mul2(m.i[3], m.i[8])));
+    const P c1i = sub2(add2(mul2(m.r[5], m.i[6]), mul2(m.i[5], m.r[6])), add2(mul2(m.r[3], m.i[8]), mul2(m.i[3], m.r[8])));
+    const P c2r = sub2(sub2(mul2(m.r[3], m.r[7]), mul2(m.i[3], m.i[7])), sub2(mul2(m.r[4], m.r[6]), mul2(m.i[4], m.i[6])));
+    const P c2i = sub2(add2(mul2(m.r[3], m.i[7]), mul2(m.i[3], m.r[7])), add2(mul2(m.r[4], m.i[6]), mul2(m.i[4], m.r[6])));
+    P di = mul2(m.r[0], c0i);
+    di = fma2(m.i[0], c0r, di);
+    di = fma2(m.r[1], c1i, di);
+    di = fma2(m.i[1], c1r, di);
+    di = fma2(m.r[2], c2i, di);
+    di = fma2(m.i[2], c2r, di);
+    // m <- m (1 - i phi / 3), phi = Im det
+    const P t = mul2(di, bc(1.f / 3.f)), nt = neg2(t);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const P re = fma2(t, m.i[k], m.r[k]);
+        m.i[k] = fma2(nt, m.r[k], m.i[k]);
+        m.r[k] = re;
     }
 }
 
