@@ -179,16 +179,17 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
-def traffic_for(workload):
-    """DRAM bytes per launch of the leapfrog kernel from the committed ncu summary."""
+def traffic_for(workload, key="dram_bytes_per_launch"):
+    """DRAM bytes per launch of the leapfrog kernel (or another figure, `key`)
+    from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
         v = d.get(workload)
         if isinstance(v, dict):
-            return v.get("dram_bytes_per_launch")
-        return v
+            return v.get(key)
+        return v if key == "dram_bytes_per_launch" else None
     return None
 
 
@@ -748,6 +749,13 @@ def main():
                 "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_link": w["bpl"], "links_per_launch": links,
                 "kernel": kname, "launch_ms": t_launch * 1000.0, "launch_ms_one_by_one": t_each * 1000.0}
+    # the FP32 FMA pipe's floor for the same launch (ncu FMA-pipe time at 100 %
+    # busy): the kernel is bound by it before HBM, so its fraction is beside the HBM one
+    fma_floor = traffic_for(args.workload, "fma_pipe_floor_ms")
+    if fma_floor:
+        roofline["fma_pipe_floor_ms"] = fma_floor
+        roofline["frac_of_fma_pipe_floor"] = fma_floor / (t_launch * 1000.0)
+        roofline["hbm_frac_at_fma_pipe_floor"] = achieved * (t_launch * 1000.0) / fma_floor / peak
 
     # ---- the BulkQuantities reduction (one pass: E^2, B^2 from U and Unext, Gauss, rho^2)
     h.set_profiling(True)
