@@ -61,8 +61,15 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BEvent<R> *__res
             const R *U = e.B[rd];
             R *Un = e.B[wr];
             for (I s = first; s < (I)e.L.V; s += stride) {
-                if (reunit) update_site<NC, R, false, true, I>(U, e.E, nullptr, Un, e.L, s);
-                else update_site<NC, R, false, false, I>(U, e.E, nullptr, Un, e.L, s);
+                // SU(2): the plane-by-plane staple sums, as the flat schedule and
+                // the single-lattice kernel (so that every schedule gives the same bits)
+                if constexpr (NC == 2) {
+                    if (reunit) update_site_su2_planes<R, false, true, I>(U, e.E, nullptr, Un, e.L, s);
+                    else update_site_su2_planes<R, false, false, I>(U, e.E, nullptr, Un, e.L, s);
+                } else {
+                    if (reunit) update_site<NC, R, false, true, I>(U, e.E, nullptr, Un, e.L, s);
+                    else update_site<NC, R, false, false, I>(U, e.E, nullptr, Un, e.L, s);
+                }
             }
         }
         cluster.sync();
@@ -121,9 +128,9 @@ __device__ __forceinline__ int flat_event(const int *__restrict__ bstart, int ne
 }
 
 // blocks of 256 threads per SM the generic flat kernel is compiled for (SU(2)
-// FP32: 40 registers, as the single-lattice kernel)
+// FP32: 64 registers, as the single-lattice kernel)
 template <int NC, typename R> struct FlatBounds { static constexpr int minb = 1; };
-template <> struct FlatBounds<2, float> { static constexpr int minb = 6; };
+template <> struct FlatBounds<2, float> { static constexpr int minb = 4; };
 
 template <int NC, typename R, typename I, bool REUNIT>
 __global__ void __launch_bounds__(256, FlatBounds<NC, R>::minb) k_batch_flat(const BEvent<R> *__restrict__ ev, const int *__restrict__ order,
@@ -132,7 +139,8 @@ __global__ void __launch_bounds__(256, FlatBounds<NC, R>::minb) k_batch_flat(con
     const BEvent<R> &e = ev[order[q]];
     const I s = (I)((int)blockIdx.x - bstart[q]) * (I)blockDim.x + (I)threadIdx.x;
     if (s >= (I)e.L.V) return;
-    update_site<NC, R, false, REUNIT, I>(e.B[rd], e.E, nullptr, e.B[rd ^ 1], e.L, s);
+    if constexpr (NC == 2) update_site_su2_planes<R, false, REUNIT, I>(e.B[rd], e.E, nullptr, e.B[rd ^ 1], e.L, s);
+    else update_site<NC, R, false, REUNIT, I>(e.B[rd], e.E, nullptr, e.B[rd ^ 1], e.L, s);
 }
 
 // SU(3) FP32, paired: thread slot t of an event covers sa = 64 (t / 32) + t % 32, sb = sa + 32

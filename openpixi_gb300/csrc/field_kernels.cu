@@ -28,10 +28,10 @@ int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 
 template <int NC, typename R> struct UpdateBounds { static constexpr int minb = 4; };
 template <> struct UpdateBounds<3, double> { static constexpr int minb = 3; };
-// SU(2) FP32 is latency-bound on its link loads: 12 blocks per SM (40
-// registers, 48 warps) instead of 9 (56 registers) took a 128^3 step from
-// 0.092 to 0.085 ms
-template <> struct UpdateBounds<2, float> { static constexpr int minb = 12; };
+// SU(2) FP32 is latency-bound on its link loads: the plane-by-plane staple sums
+// at 8 blocks per SM (64 registers) take a 128^3 step in 0.081 ms (0.085 ms
+// for the per-link sums at 12 blocks and 40 registers, 0.092 ms at 56)
+template <> struct UpdateBounds<2, float> { static constexpr int minb = 8; };
 
 template <int NC, typename R, bool HAS_J, bool REUNIT, typename I, bool PLANES = false>
 __global__ void __launch_bounds__(128, UpdateBounds<NC, R>::minb)
@@ -40,7 +40,7 @@ k_update_grid(const R *__restrict__ U, R *__restrict__ E, const R *__restrict__ 
     const I s = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
     if (s >= (I)L.V) return;
     if (active && !active[s]) return;  // Cell.isActive gate (FastTYMSolver.java:51)
-    if constexpr (NC == 2 && sizeof(R) == 8) {
+    if constexpr (NC == 2) {
         if (PLANES) {
             update_site_su2_planes<R, HAS_J, REUNIT, I>(U, E, J, Unext, L, s);
             return;
@@ -431,9 +431,9 @@ static void update_grid_su3f_pair(Ctx &c, bool reunit) {
 
 template <int NC, typename R, typename I>
 static void launch_update_grid_i(Ctx &c, bool reunit, dim3 grid, int B, const R *U, R *E, const R *J, R *Un) {
-    // SU(2) FP64: the plane-by-plane staple sums (update_site_su2_planes, 6 %
-    // faster on the FP64 pipe); SU(2) FP32 keeps update_site (40 registers)
-    if (NC == 2 && sizeof(R) == 8) {
+    // SU(2): the plane-by-plane staple sums (update_site_su2_planes: 6 % faster
+    // in FP64, 5 % in FP32)
+    if (NC == 2) {
         if (c.j_nonzero) {
             if (reunit) k_update_grid<NC, R, true, true, I, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
             else k_update_grid<NC, R, true, false, I, true><<<grid, B, 0, c.stream>>>(U, E, J, Un, c.active, c.L);
