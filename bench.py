@@ -660,6 +660,37 @@ def bench_configs(device):
     return out
 
 
+# the lattice-size sweep: (ncolors, precision, reunit_every, sigma, bytes per link update, L)
+SWEEP = [(3, "f32", 10, 0.2, 208, (48, 64, 96, 128, 160, 192, 256)),
+         (2, "f32", 10, 0.1, 56, (64, 128, 192, 256)),
+         (2, "f64", 0, 0.1, 112, (32, 128))]
+
+
+def bench_sweep(device, steps=50, warmup=5):
+    """Lattice-size sweep of the single-lattice leapfrog: per form and L^3
+    periodic lattice (dt = 0.05, seeded fields), the best of three
+    opx_time_steps runs (CUDA events on the handle's stream) of `steps` steps
+    after `warmup` steps; one JSON line per row, with the fraction of the
+    measured copy bandwidth at the form's algorithmic bytes per link update."""
+    import openpixi_gb300 as opx
+    from openpixi_gb300 import _native as N
+    peak, peak_kind = hbm_peak()
+    for nc, prec, reunit, sigma, bpl, sizes in SWEEP:
+        for L in sizes:
+            h = opx.Handle(nc, (L, L, L), dt=0.05, precision=N.OPX_F32 if prec == "f32" else N.OPX_F64,
+                           reunit_every=reunit, device=device)
+            h.init_random(SEED, sigma, sigma)
+            h.initialize()
+            h.step(warmup)
+            ms = min(h.time_steps(steps) for _ in range(3)) / steps
+            links = 3 * L ** 3
+            print(json.dumps({"form": f"SU({nc}) {prec.upper()}", "L": L, "ms_per_step": ms,
+                              "g_link_updates_per_s": links / ms / 1e6,
+                              "hbm_roofline_frac": bpl * links / (ms * 1e-3) / (peak * 1e9),
+                              "bytes_per_link_update": bpl, "peak_gbs": peak, "peak": peak_kind}), flush=True)
+            h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -674,8 +705,9 @@ def main():
     ap.add_argument("--no-configs", action="store_true")
     # one leg alone (profiling runs): the CPIC collision (`--leg-steps` steps with
     # its diagnostics, no oracle check) or the batched form (SU(`--batch-nc`),
-    # `--batch-events` events, `--leg-steps` steps); prints that leg's JSON
-    ap.add_argument("--leg", default="all", choices=["all", "cgc", "batch"])
+    # `--batch-events` events, `--leg-steps` steps); prints that leg's JSON.
+    # `--leg sweep`: the lattice-size sweep, one JSON line per form and size
+    ap.add_argument("--leg", default="all", choices=["all", "cgc", "batch", "sweep"])
     ap.add_argument("--leg-steps", type=int, default=20)
     ap.add_argument("--batch-nc", type=int, default=3, choices=[2, 3])
     ap.add_argument("--batch-events", type=int, default=64)
@@ -685,6 +717,9 @@ def main():
         return 0
     if args.leg == "batch":
         print(json.dumps(bench_batch(0, nc=args.batch_nc, nsteps=args.leg_steps, nev=args.batch_events)), flush=True)
+        return 0
+    if args.leg == "sweep":
+        bench_sweep(0)
         return 0
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
