@@ -21,13 +21,6 @@ namespace pr {
 
 typedef float2 P;
 
-// 1/k for the exponential series (t_k = t_{k-1} / k), read with a uniform index
-static __constant__ float c_inv_k[40] = {
-    0.f,         1.f,         1.f / 2,  1.f / 3,  1.f / 4,  1.f / 5,  1.f / 6,  1.f / 7,  1.f / 8,  1.f / 9,
-    1.f / 10,    1.f / 11,    1.f / 12, 1.f / 13, 1.f / 14, 1.f / 15, 1.f / 16, 1.f / 17, 1.f / 18, 1.f / 19,
-    1.f / 20,    1.f / 21,    1.f / 22, 1.f / 23, 1.f / 24, 1.f / 25, 1.f / 26, 1.f / 27, 1.f / 28, 1.f / 29,
-    1.f / 30,    1.f / 31,    1.f / 32, 1.f / 33, 1.f / 34, 1.f / 35, 1.f / 36, 1.f / 37, 1.f / 38, 1.f / 39};
-
 __device__ __forceinline__ P pp(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ P bc(float a) { return make_float2(a, a); }
 __device__ __forceinline__ P fma2(P a, P b, P c) { return __ffma2_rn(a, b, c); }
@@ -240,20 +233,22 @@ __device__ __forceinline__ M expi(const P *x) {
     const P two_c1 = add2(c1, c1);
     const P nrm = pp(sqrtf(two_c1.x), sqrtf(two_c1.y));
     P bound = bc(1.f);
-    for (int k = 1; k < 40; k++) {
-        const P nal = mul2(c0, ga), nbe = fma2(c1, ga, al);
-        ga = be;
-        al = nal;
-        be = nbe;
-        t = t * c_inv_k[k];
-        const P T = bc(t), mT = bc(-t);
-        switch (k & 3) {
-        case 0: f0r = fma2(T, al, f0r); f1r = fma2(T, be, f1r); f2r = fma2(T, ga, f2r); break;
-        case 1: f0i = fma2(T, al, f0i); f1i = fma2(T, be, f1i); f2i = fma2(T, ga, f2i); break;
-        case 2: f0r = fma2(mT, al, f0r); f1r = fma2(mT, be, f1r); f2r = fma2(mT, ga, f2r); break;
-        default: f0i = fma2(mT, al, f0i); f1i = fma2(mT, be, f1i); f2i = fma2(mT, ga, f2i); break;
+    const P nrm2 = mul2(nrm, nrm), nrm4 = mul2(nrm2, nrm2);
+    // four terms per pass, i^k fixed within a pass (k = 1, 2, 3, 0 mod 4), the
+    // stopping test after the fourth
+    for (int k = 1; k < 40; k += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const P nal = mul2(c0, ga), nbe = fma2(c1, ga, al);
+            ga = be;
+            al = nal;
+            be = nbe;
+            t = t * c_inv_k32[k + u];
+            const P T = bc((u == 1 || u == 2) ? -t : t);
+            if (u & 1) { f0r = fma2(T, al, f0r); f1r = fma2(T, be, f1r); f2r = fma2(T, ga, f2r); }
+            else { f0i = fma2(T, al, f0i); f1i = fma2(T, be, f1i); f2i = fma2(T, ga, f2i); }
         }
-        bound = mul2(bound, nrm);
+        bound = mul2(bound, nrm4);
         if (maxl(bound) * t < 5.9604645e-08f * 0.01f) break;
     }
     // Q = H^2 (hermitian)
