@@ -529,7 +529,7 @@ static int ensure_measure_buffers(Ctx &c, int nsteps) {
     if (ok && !c.meas_part) {
         // the partials of up to 64 steps (at most 64 MB): their rows are formed
         // with one launch per chunk of steps
-        const size_t per_step = sizeof(double) * MEAS_ROW * measured_blocks(c);
+        const size_t per_step = sizeof(double) * MEAS_ROW * measured_parts(c);
         c.meas_chunk = (int)std::max<size_t>(1, std::min<size_t>(64, ((size_t)64 << 20) / per_step));
         ok = cudaMalloc((void **)&c.meas_part, per_step * c.meas_chunk) == cudaSuccess;
         if (!ok) c.meas_chunk = 0;
@@ -567,7 +567,7 @@ int opx_step_measured(opx_ctx *ctx, int nsteps, opx_observables *out) {
     int rc = ensure_measure_buffers(c, nsteps);
     if (rc) return rc;
     c.bcache.calls = -1;
-    const size_t per_step = (size_t)MEAS_ROW * measured_blocks(c);
+    const size_t per_step = (size_t)MEAS_ROW * measured_parts(c);
     for (int k0 = 0; k0 < nsteps; k0 += c.meas_chunk) {
         const int nk = std::min(c.meas_chunk, nsteps - k0);
         phase_begin(c);

@@ -85,16 +85,18 @@ k_update_grid_su3f_pair(const float *__restrict__ U, float *__restrict__ E, cons
 // The measured step: the update above plus the per-site BulkQuantities terms
 // it can form from what it loads (update_site_pair with MEAS) and the Gauss
 // law of the previous state from the previous step's transported terms Win
-// (gauss_w_pair); it stores its own in Wout.  Every thread reaches the block
-// reduction, so no thread returns early.  Block partials: FP32 warp sums,
-// combined per block in FP64 and in a fixed order; part[block][MEAS_COLS].
+// (gauss_w_pair); it stores its own in Wout.  Every thread reaches the warp
+// reduction, so no thread returns early.  Partials: FP32 warp sums, one row per
+// warp, part[block * MEAS_THREADS / 32 + warp][MEAS_COLS].  There is no block
+// barrier: a warp that has finished leaves, and the next block can start on
+// its SM without waiting for the block's last warp (3 % per 128^3 measured
+// step against block partials combined after a barrier).
 template <typename I, bool REUNIT>
 __global__ void __launch_bounds__(MEAS_THREADS, 3)
 k_update_measure_su3f_pair(const float *__restrict__ U, float *__restrict__ E, float *__restrict__ Eout,
                            const float *__restrict__ Win, float *__restrict__ Wout, const float *__restrict__ rho,
                            float *__restrict__ Unext, Lat L, double *__restrict__ part) {
     __shared__ float slots[MEAS_COLS * MEAS_THREADS];
-    __shared__ double warp_sums[MEAS_COLS][MEAS_THREADS / 32];
     float *slot = slots + threadIdx.x;
 #pragma unroll
     for (int q = 0; q < MEAS_COLS; q++) slot[q * MEAS_THREADS] = 0.f;
@@ -108,23 +110,17 @@ k_update_measure_su3f_pair(const float *__restrict__ U, float *__restrict__ E, f
         update_site_pair<I, false, REUNIT, true>(U, E, nullptr, Unext, L, sa, sb, true, vb, Eout, slot, Wout);
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double *pw = part + ((long)blockIdx.x * (MEAS_THREADS / 32) + w) * MEAS_COLS;
 #pragma unroll
     for (int q = 0; q < MEAS_COLS; q++) {
         float v = slot[q * MEAS_THREADS];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) warp_sums[q][w] = (double)v;
-    }
-    __syncthreads();
-    if (threadIdx.x < MEAS_COLS) {
-        double v = 0.0;
-#pragma unroll
-        for (int k = 0; k < MEAS_THREADS / 32; k++) v += warp_sums[threadIdx.x][k];
-        part[(long)blockIdx.x * MEAS_COLS + threadIdx.x] = v;
+        if (lane == 0) pw[q] = (double)v;
     }
 }
 
-// Column sums of the block partials in a fixed order (block (q, k): column q
+// Column sums of the warp partials in a fixed order (block (q, k): column q
 // of step k of the chunk), with the unit factors of the BulkQuantities
 // columns: (g a_i)^-2 for E^2, (g a_i)^-2 / 2 for B^2 (the U / Unext
 // average).  part[k][nparts][MEAS_COLS] -> rows[k][8].
@@ -158,8 +154,10 @@ bool measured_step_fusable(const Ctx &c) {
 }
 
 int measured_blocks(const Ctx &c) { return grid_for(((c.L.V + 63) / 64) * 32, MEAS_THREADS); }
+// rows of partials per measured step (one per warp)
+int measured_parts(const Ctx &c) { return measured_blocks(c) * (MEAS_THREADS / 32); }
 
-// One measured step, block partials into part[measured_blocks][MEAS_COLS]:
+// One measured step, warp partials into part[measured_parts][MEAS_COLS]:
 // reads c.U, c.E and Win, writes c.Unext, Eout and Wout (the caller swaps Eout
 // into c.E and Wout into Win).
 void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, void *Wout, double *part) {
@@ -179,7 +177,7 @@ void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, voi
 
 // The rows of nsteps measured steps from their consecutive partials.
 void launch_measure_combine(Ctx &c, const double *part, int nsteps, double *rows) {
-    k_measure_combine<<<dim3(MEAS_COLS, nsteps), 256, 0, c.stream>>>(part, measured_blocks(c), c.L, rows);
+    k_measure_combine<<<dim3(MEAS_COLS, nsteps), 256, 0, c.stream>>>(part, measured_parts(c), c.L, rows);
     c.launches += 1;
 }
 

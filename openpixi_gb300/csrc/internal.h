@@ -147,6 +147,7 @@ void launch_reunit(Ctx &c, void *links);
 constexpr int MEAS_ROW = 7;
 bool measured_step_fusable(const Ctx &c);
 int measured_blocks(const Ctx &c);
+int measured_parts(const Ctx &c);
 void launch_update_measure(Ctx &c, bool reunit, void *Eout, const void *Win, void *Wout, double *part);
 void launch_measure_combine(Ctx &c, const double *part, int nsteps, double *rows);  // rows[nsteps][8]
 // ---- reductions (reduce_kernels.cu) ----
