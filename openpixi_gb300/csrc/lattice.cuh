@@ -34,7 +34,22 @@ struct Lat {
     // Grid.getB area factor a_d / (a_j a_k) and Gauss-law factor 1 / (a_i g a_i)
     double bfac[3], gfac[3];
     float bfacf[3], gfacf[3];
+    // division by N2 (k = 0) and N1 (k = 1) of site indices below 2^31 as a
+    // multiply and a shift: s / N = (s * dmul[k]) >> dsh[k] (div_n)
+    unsigned dmul[2];
+    int dsh[2];
 };
+
+// m = ceil(2^(31 + l) / n), l = ceil(log2 n): then floor(s m / 2^(31 + l)) =
+// floor(s / n) for every s < 2^31 (the round-up method of Granlund and
+// Montgomery: s m / 2^(31 + l) exceeds s / n by less than 1 / n), and m < 2^32.
+__host__ inline void div_magic(int n, unsigned *m, int *sh) {
+    int l = 0;
+    while ((1L << l) < n) l++;
+    const unsigned long long p = 1ULL << (31 + l);
+    *m = (unsigned)((p + (unsigned long long)n - 1) / (unsigned long long)n);
+    *sh = 31 + l;
+}
 
 __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double g) {
     Lat L;
@@ -59,6 +74,8 @@ __host__ inline Lat make_lat(const int *dims, const double *a, double dt, double
         L.bfacf[d] = (float)L.bfac[d];
         L.gfacf[d] = (float)L.gfac[d];
     }
+    div_magic(dims[2], &L.dmul[0], &L.dsh[0]);
+    div_magic(dims[1], &L.dmul[1], &L.dsh[1]);
     return L;
 }
 
@@ -100,13 +117,20 @@ struct Nbr {
     long bwd[3];  // index of x - d
 };
 
-// Coordinates of site s; I = int where the site index fits (32-bit divisions
-// are several times cheaper than 64-bit ones).
+// floor(s / N2) (k = 0) or floor(s / N1) (k = 1) for 0 <= s < 2^31
+__device__ __forceinline__ int div_n(const Lat &L, int k, int s) {
+    return (int)(((unsigned long long)(unsigned)s * (unsigned long long)L.dmul[k]) >> L.dsh[k]);
+}
+// Coordinates of site s; I = int where the site index fits (then without a
+// division: div_n), 64-bit divisions otherwise.
 template <typename I>
 __device__ __forceinline__ void site_coords(const Lat &L, I s, int *x) {
-    const I t = s / (I)L.n[2];
+    I t, u;
+    if constexpr (sizeof(I) == 4) t = (I)div_n(L, 0, (int)s);
+    else t = s / (I)L.n[2];
     x[2] = (int)(s - t * (I)L.n[2]);
-    const I u = t / (I)L.n[1];
+    if constexpr (sizeof(I) == 4) u = (I)div_n(L, 1, (int)t);
+    else u = t / (I)L.n[1];
     x[1] = (int)(t - u * (I)L.n[1]);
     x[0] = (int)u;
 }

@@ -595,13 +595,7 @@ template <typename I> __device__ __forceinline__ I shift(const Lat &L, I s, int 
     if (o > 0) return xd == nd - 1 ? s - (I)(nd - 1) * st : s + st;
     return xd == 0 ? s + (I)(nd - 1) * st : s - st;
 }
-template <typename I> __device__ __forceinline__ void coords(const Lat &L, I s, int *x) {
-    const I t = s / (I)L.n[2];
-    x[2] = (int)(s - t * (I)L.n[2]);
-    const I u = t / (I)L.n[1];
-    x[1] = (int)(t - u * (I)L.n[1]);
-    x[0] = (int)u;
-}
+template <typename I> __device__ __forceinline__ void coords(const Lat &L, I s, int *x) { site_coords<I>(L, s, x); }
 
 }  // namespace pr
 
