@@ -118,7 +118,7 @@ struct Nbr {
 };
 
 // floor(s / N2) (k = 0) or floor(s / N1) (k = 1) for 0 <= s < 2^31
-__device__ __forceinline__ int div_n(const Lat &L, int k, int s) {
+OPX_HD OPX_INLINE int div_n(const Lat &L, int k, int s) {
     return (int)(((unsigned long long)(unsigned)s * (unsigned long long)L.dmul[k]) >> L.dsh[k]);
 }
 // Coordinates of site s; I = int where the site index fits (then without a
