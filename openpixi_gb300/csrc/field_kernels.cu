@@ -153,6 +153,8 @@ bool measured_step_fusable(const Ctx &c) {
            !c.eval && c.P.n == 0 && c.sg.empty();
 }
 
+// the host sizes the partials by MEAS_ROW, the kernel writes MEAS_COLS per warp
+static_assert(MEAS_ROW == MEAS_COLS, "measured-step row width");
 int measured_blocks(const Ctx &c) { return grid_for(((c.L.V + 63) / 64) * 32, MEAS_THREADS); }
 // rows of partials per measured step (one per warp)
 int measured_parts(const Ctx &c) { return measured_blocks(c) * (MEAS_THREADS / 32); }
